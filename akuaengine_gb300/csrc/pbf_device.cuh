@@ -1,0 +1,137 @@
+// Device-side parameters and pair math of the PBF step.
+//
+// Compiled with --fmad=false: no multiply-add is fused unless written as __fmaf_rn.  The explicit
+// fusions below are the ones the CUDA compiler applies by default to the reference's expressions
+// (a product whose only use is an addend: a*b + c -> fma(a, b, c); for a sum of two products the
+// first product is fused), so a step here rounds like the reference's wherever it uses the same
+// operations.  The reference's powf calls with integer exponents (SmoothingKernelsCUDA.h:20,27 and
+// the artificial-pressure power, ConstraintSolverCUDA.cu:124) are multiplications here.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace akua {
+
+// Everything a kernel of one step reads besides the particle arrays.  Lives in device memory and is
+// rewritten by a one-thread kernel at the start of every step, so a captured step graph replays
+// with new dt / box / gravity without re-capture.
+struct StepParams {
+    // PBFConfig-derived constants
+    float h;            // smoothRadius
+    float h2;           // h*h in float (SmoothingKernelsCUDA.h:17, NeighbourSearchCUDA.cu:90)
+    float kp;           // 315 / (64 * 3.14f * h^9), evaluated in double and rounded
+    float ks;           // -45 / (3.14f * h^6), evaluated in double and rounded
+    float w0;           // poly6(0)
+    float inv_rho0;     // 1.0f / restDensity (ConstraintSolverCUDA.cu:201)
+    float relaxation;
+    float wdq;          // poly6(delta_q^2)
+    float neg_k;        // -k
+    float corr_n;       // n (float)
+    int32_t corr_n_int; // n when it is an integer in [0, 64], else -1
+    float hash_cell;    // cell size of the hash keys (smoothRadius, NeighbourSearchCUDA.cu:163)
+    float search_cell;  // cell size of the neighbour walk (spatialHashCellSize)
+    float vort_eps;
+    float visc;
+    // per step
+    float dt;
+    float gravity[3];
+    float box_min[3];
+    float box_max[3];
+    float neg_restitution;  // -e
+    float keep;             // 1 - friction, in float
+    // sizes
+    int32_t n;
+    int32_t cap;
+    uint32_t table_size;
+};
+
+__device__ __forceinline__ float fmaf_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+
+// glm::dot(vec3, vec3) = tmp.x + tmp.y + tmp.z with tmp = a*b, contracted.
+__device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, float by, float bz) {
+    return __fmaf_rn(az, bz, __fmaf_rn(ax, bx, ay * by));
+}
+__device__ __forceinline__ float len2(float x, float y, float z) { return dot3(x, y, z, x, y, z); }
+
+// MathUtilsCUDA::cross, contracted: fma(a.y, b.z, -(a.z*b.y)) etc.
+__device__ __forceinline__ float3 cross3(float ax, float ay, float az, float bx, float by, float bz) {
+    return make_float3(__fmaf_rn(ay, bz, -(az * by)), __fmaf_rn(az, bx, -(ax * bz)),
+                       __fmaf_rn(ax, by, -(ay * bx)));
+}
+
+// Cell coordinate: floorf(x / cell) with an IEEE divide (NeighbourSearchCUDA.cu:15-21).
+__device__ __forceinline__ int cell_coord(float x, float cell) {
+    return static_cast<int>(floorf(__fdiv_rn(x, cell)));
+}
+
+// NeighbourSearchCUDA.cu:23-27: int products wrap, u32 xor, then % tableSize as u32.
+__device__ __forceinline__ uint32_t cell_hash(int cx, int cy, int cz, uint32_t table) {
+    const uint32_t hx = static_cast<uint32_t>(cx) * 73856093u;
+    const uint32_t hy = static_cast<uint32_t>(cy) * 19349663u;
+    const uint32_t hz = static_cast<uint32_t>(cz) * 83492791u;
+    return (hx ^ hy ^ hz) % table;
+}
+
+// poly6 (SmoothingKernelsCUDA.h:16-21): 0 when r2 > h2, else kp * (h2 - r2)^3.
+__device__ __forceinline__ float poly6(const StepParams& p, float r2) {
+    const float d = p.h2 - r2;
+    const float w = p.kp * ((d * d) * d);
+    return r2 > p.h2 ? 0.0f : w;
+}
+
+// Gradient of the spiky kernel (SmoothingKernelsCUDA.h:23-28): zero when |r| > h or |r| < 1e-5,
+// else ks * (h - |r|)^2 * r / |r|.  EXACT: IEEE sqrt and three IEEE divides, as the reference.
+// Fast: one reciprocal square root; the thresholds are tested on r^2.
+template <bool EXACT>
+__device__ __forceinline__ float3 spiky_grad(const StepParams& p, float sx, float sy, float sz) {
+    const float r2 = len2(sx, sy, sz);
+    if constexpr (EXACT) {
+        const float r = __fsqrt_rn(r2);
+        if (r > p.h || r < 1e-5f) return make_float3(0.f, 0.f, 0.f);
+        const float q = p.h - r;
+        const float c = p.ks * (q * q);
+        return make_float3(__fdiv_rn(c * sx, r), __fdiv_rn(c * sy, r), __fdiv_rn(c * sz, r));
+    } else {
+        const float ir = rsqrtf(r2);
+        const float r = r2 * ir;
+        const float q = p.h - r;
+        const float c = (r2 > p.h2 || r2 < 1e-10f) ? 0.0f : p.ks * (q * q) * ir;
+        return make_float3(c * sx, c * sy, c * sz);
+    }
+}
+
+// Integer power by binary exponentiation (same multiplication pattern as the host restatement).
+__device__ __forceinline__ float pown(float x, int n) {
+    float result = 1.0f;
+    float base = x;
+    bool first = true;
+    while (n > 0) {
+        if (n & 1) {
+            result = first ? base : result * base;
+            first = false;
+        }
+        n >>= 1;
+        if (n) base = base * base;
+    }
+    return result;
+}
+
+// Artificial pressure s_corr = -k * (W(r2) / W(dq^2))^n (ConstraintSolverCUDA.cu:123-124).
+template <bool EXACT>
+__device__ __forceinline__ float scorr(const StepParams& p, float r2) {
+    const float w = poly6(p, r2);
+    const float ratio = EXACT ? __fdiv_rn(w, p.wdq) : __fdividef(w, p.wdq);
+    float pw;
+    if (p.corr_n_int == 4) {
+        const float r_2 = ratio * ratio;
+        pw = r_2 * r_2;
+    } else if (p.corr_n_int >= 0) {
+        pw = pown(ratio, p.corr_n_int);
+    } else {
+        pw = powf(ratio, p.corr_n);
+    }
+    return p.neg_k * pw;
+}
+
+}  // namespace akua

@@ -1,0 +1,686 @@
+// Host side of the GB300 PBF step: device memory, the per-step launch sequence, CUDA-graph
+// capture and the C ABI declared in include/akua_pbf.h.
+//
+// One handle = one particle set on one device.  A step is: [params] [import] then the captured
+// body: predict+hash -> radix sort -> gather -> bucket table -> neighbour walk (+ iteration 1
+// density/lambda) -> (delta+correct, density+lambda) x iterations -> delta+update+damping ->
+// vorticity -> confinement -> XSPH -> export.  Nothing on this path copies to the host or
+// synchronises; the reference instead synchronises after every kernel and moves the neighbour
+// lists through host memory four times per step (PBFSolver.h:23-24, NeighbourSearchCUDA.cu:151-154,
+// 182-183, ConstraintSolverCUDA.cu:195-198, IntegrationCUDA.cu:269-272).
+#include <climits>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "akua_pbf.h"
+#include "pbf_kernels.cuh"
+#include "radix_sort.cuh"
+
+using akua::StepParams;
+
+struct akua_pbf {
+    int device = 0;
+    int n = 0;
+    akua_pbf_config cfg{};
+    akua_lambda_corr_params corr{};
+    uint32_t table_size = 0;
+    uint32_t table_alloc = 0;
+    float restitution = 0.0f;
+    float friction = 0.95f;
+    uint32_t options = 0;
+    cudaStream_t stream = nullptr;          // caller's stream (nullptr = legacy default stream)
+    cudaStream_t capture_stream = nullptr;  // private stream used only for graph capture
+    char* attached = nullptr;
+    size_t stride = 0;
+    bool state_valid = false;  // device state holds the particles (resident mode)
+
+    StepParams* d_params = nullptr;
+    float4 *x4 = nullptr, *v4 = nullptr, *col4 = nullptr;
+    float4 *x4g = nullptr, *v4g = nullptr, *col4g = nullptr;
+    float4 *ps0 = nullptr, *ps1 = nullptr, *dp4 = nullptr, *dpg = nullptr;
+    float4 *vstar4 = nullptr, *om4 = nullptr, *vc4 = nullptr;
+    float *size = nullptr, *sizeg = nullptr, *rho = nullptr, *lam = nullptr;
+    float *rhog = nullptr, *lamg = nullptr;
+    uint32_t *keys0 = nullptr, *vals0 = nullptr, *keys1 = nullptr, *vals1 = nullptr;
+    uint32_t *table = nullptr, *nbr = nullptr, *cnt = nullptr, *counts = nullptr, *flags = nullptr;
+    uint32_t *sorted_keys = nullptr, *sorted_perm = nullptr;
+    int passes = 0;
+    char* staging = nullptr;
+    size_t staging_bytes = 0;
+
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool graph_ok = false;
+    uint32_t graph_options = 0;
+    const char* graph_aos = nullptr;
+    size_t graph_stride = 0;
+    int graph_captures = 0;
+    int body_launches = 0;
+
+    int64_t steps = 0;
+    uint64_t device_bytes = 0;
+
+    // profiling (akua_pbf_profile_begin/end): one event after every kernel of a step
+    bool prof_active = false;
+    int prof_steps_left = 0;
+    std::vector<cudaEvent_t> prof_events;
+    std::vector<const char*> prof_names;  // nullptr marks the start of a step
+    size_t prof_next = 0;
+};
+
+namespace {
+
+int cuda_status(cudaError_t e) {
+    if (e == cudaSuccess) return AKUA_OK;
+    if (e == cudaErrorMemoryAllocation) return AKUA_ERR_OUT_OF_MEMORY;
+    return AKUA_ERR_CUDA;
+}
+
+template <class T>
+cudaError_t dalloc(akua_pbf* s, T** p, size_t count) {
+    const size_t bytes = count * sizeof(T);
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), bytes > 0 ? bytes : sizeof(T));
+    if (e == cudaSuccess) s->device_bytes += bytes;
+    return e;
+}
+
+void free_all(akua_pbf* s) {
+    void* ptrs[] = {s->d_params, s->x4, s->v4, s->col4, s->x4g, s->v4g, s->col4g, s->ps0, s->ps1,
+                    s->dp4, s->dpg, s->vstar4, s->om4, s->vc4, s->size, s->sizeg, s->rho, s->lam,
+                    s->rhog, s->lamg, s->keys0, s->vals0, s->keys1, s->vals1, s->table, s->nbr,
+                    s->cnt, s->counts, s->flags, s->staging};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (s->exec) cudaGraphExecDestroy(s->exec);
+    if (s->graph) cudaGraphDestroy(s->graph);
+    if (s->capture_stream) cudaStreamDestroy(s->capture_stream);
+}
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) cudaSetDevice(dev);
+        else prev = -1;
+    }
+    ~DeviceGuard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+bool finite3(const float* v) {
+    return v && std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]);
+}
+
+// Kernel constants, evaluated once per step on the host in the order the device and the host
+// restatement use.  Host code is compiled with -ffp-contract=off.
+StepParams make_params(const akua_pbf* s, float dt, const float* bmin, const float* bmax) {
+    StepParams p{};
+    const float h = s->cfg.smoothRadius;
+    p.h = h;
+    p.h2 = h * h;
+    const double pi_ref = (double)3.14f;  // SmoothingKernelsCUDA.h:20,27 write pi as 3.14f
+    const double hd = (double)h;
+    const double h2 = hd * hd, h3 = h2 * hd, h6 = h3 * h3, h9 = h6 * h3;
+    p.kp = (float)(315.0 / (64.0 * pi_ref * h9));
+    p.ks = (float)(-(45.0 / (pi_ref * h6)));
+    {
+        const float d = p.h2 - 0.0f;
+        p.w0 = p.kp * ((d * d) * d);
+    }
+    p.inv_rho0 = 1.0f / s->cfg.restDensity;
+    p.relaxation = s->cfg.relaxation;
+    {
+        const float dq2 = s->corr.delta_q * s->corr.delta_q;
+        const float d = p.h2 - dq2;
+        p.wdq = dq2 > p.h2 ? 0.0f : p.kp * ((d * d) * d);
+    }
+    p.neg_k = -s->corr.k;
+    p.corr_n = s->corr.n;
+    const float nf = s->corr.n;
+    p.corr_n_int = (std::floor(nf) == nf && nf >= 0.0f && nf <= 64.0f) ? (int32_t)nf : -1;
+    p.hash_cell = h;  // the reference hashes with the smoothing radius (NeighbourSearchCUDA.cu:163)
+    p.search_cell = s->cfg.spatialHashCellSize;
+    p.vort_eps = s->cfg.vorticityEpsilon;
+    p.visc = s->cfg.viscosity;
+    p.dt = dt;
+    for (int a = 0; a < 3; ++a) {
+        p.gravity[a] = s->cfg.gravity[a];
+        p.box_min[a] = bmin[a];
+        p.box_max[a] = bmax[a];
+    }
+    p.neg_restitution = -s->restitution;
+    p.keep = 1.0f - s->friction;
+    p.n = s->n;
+    p.cap = s->cfg.maxNeighbours;
+    p.table_size = s->table_size;
+    return p;
+}
+
+inline int grid_for(int n, int block) { return (n + block - 1) / block; }
+
+// Counts launches and, while profiling (never during capture), records an event after each.
+struct Marker {
+    akua_pbf* s;
+    cudaStream_t st;
+    bool record;
+    int launches = 0;
+    void operator()(const char* name) {
+        ++launches;
+        if (record && s->prof_next < s->prof_events.size()) {
+            cudaEventRecord(s->prof_events[s->prof_next], st);
+            s->prof_names[s->prof_next] = name;
+            ++s->prof_next;
+        }
+    }
+};
+
+template <bool EXACT>
+void enqueue_pairs(akua_pbf* s, cudaStream_t st, Marker& mark) {
+    const int n = s->n;
+    const int gp = grid_for(n, akua::kPairBlock);
+    const int iters = s->cfg.solverIterations;
+    float4* ps[2] = {s->ps0, s->ps1};
+    akua::k_search<EXACT><<<gp, akua::kPairBlock, 0, st>>>(s->d_params, s->ps0, s->sorted_keys,
+                                                           s->table, s->nbr, s->cnt, s->rho, s->lam,
+                                                           s->flags, iters > 0 ? 1 : 0);
+    mark("k_search");
+    for (int it = 0; it < iters; ++it) {
+        float4* cur = ps[it & 1];
+        float4* nxt = ps[(it + 1) & 1];
+        if (it > 0) {
+            akua::k_density_lambda<EXACT><<<gp, akua::kPairBlock, 0, st>>>(s->d_params, cur, s->nbr,
+                                                                           s->cnt, s->rho, s->lam);
+            mark("k_density_lambda");
+        }
+        if (it + 1 < iters) {
+            akua::k_delta_correct<EXACT><<<gp, akua::kPairBlock, 0, st>>>(
+                s->d_params, cur, s->lam, s->nbr, s->cnt, nxt, s->dp4);
+            mark("k_delta_correct");
+        } else {
+            akua::k_delta_final<EXACT><<<gp, akua::kPairBlock, 0, st>>>(
+                s->d_params, cur, s->lam, s->nbr, s->cnt, s->x4g, s->x4, s->v4, s->vstar4, s->dp4,
+                s->col4g, s->sizeg, s->col4, s->size, 1);
+            mark("k_delta_final");
+        }
+    }
+    if (iters == 0) {
+        akua::k_delta_final<EXACT><<<gp, akua::kPairBlock, 0, st>>>(
+            s->d_params, s->ps0, s->lam, s->nbr, s->cnt, s->x4g, s->x4, s->v4, s->vstar4, s->dp4,
+            s->col4g, s->sizeg, s->col4, s->size, 0);
+        mark("k_delta_final");
+    }
+    akua::k_vorticity<EXACT><<<gp, akua::kPairBlock, 0, st>>>(s->d_params, s->x4, s->v4, s->nbr,
+                                                              s->cnt, s->om4);
+    mark("k_vorticity");
+    akua::k_confine<EXACT><<<gp, akua::kPairBlock, 0, st>>>(s->d_params, s->x4, s->v4, s->om4,
+                                                            s->rho, s->nbr, s->cnt, s->vc4);
+    mark("k_confine");
+    akua::k_xsph<<<gp, akua::kPairBlock, 0, st>>>(s->d_params, s->x4, s->vc4, s->nbr, s->cnt, s->v4);
+    mark("k_xsph");
+}
+
+// Everything of a step after the parameter upload and the import: the captured body.
+void enqueue_body(akua_pbf* s, cudaStream_t st, const char* aos, size_t stride, bool record) {
+    const int n = s->n;
+    const int ge = grid_for(n, akua::kElemBlock);
+    Marker mark{s, st, record};
+    const bool carry = s->cfg.solverIterations == 0;
+    akua::k_predict_hash<<<ge, akua::kElemBlock, 0, st>>>(s->d_params, s->x4, s->v4, s->keys0);
+    mark("k_predict_hash");
+    akua::radix::sort_pairs(st, s->keys0, s->vals0, s->keys1, s->vals1, s->counts, n, s->passes,
+                            mark);
+    akua::k_gather<<<ge, akua::kElemBlock, 0, st>>>(
+        s->d_params, s->sorted_perm, s->x4, s->v4, s->col4, s->size, s->x4g, s->v4g, s->col4g,
+        s->sizeg, s->ps0, s->rhog, s->lamg, s->dpg, s->rho, s->lam, s->dp4, carry ? 1 : 0);
+    mark("k_gather");
+    akua::k_build_table<<<ge, akua::kElemBlock, 0, st>>>(s->d_params, s->sorted_keys, s->table);
+    mark("k_build_table");
+    // v4g holds the sorted velocities; k_delta_final writes the damped ones into v4.
+    if (s->options & AKUA_PBF_OPT_EXACT_MATH) enqueue_pairs<true>(s, st, mark);
+    else enqueue_pairs<false>(s, st, mark);
+    if (aos) {
+        akua::k_export<<<ge, akua::kElemBlock, 0, st>>>(const_cast<char*>(aos), stride, n, s->x4,
+                                                        s->v4, s->vstar4, s->dp4, s->om4, s->rho,
+                                                        s->lam, s->sorted_keys, s->col4, s->size);
+        mark("k_export");
+    }
+    s->body_launches = mark.launches;
+}
+
+void update_sort_layout(akua_pbf* s) {
+    s->passes = akua::radix::passes_for(s->table_size);
+    const bool odd = (s->passes & 1) != 0;
+    s->sorted_keys = odd ? s->keys1 : s->keys0;
+    s->sorted_perm = odd ? s->vals1 : s->vals0;
+}
+
+void invalidate_graph(akua_pbf* s) {
+    if (s->exec) cudaGraphExecDestroy(s->exec);
+    if (s->graph) cudaGraphDestroy(s->graph);
+    s->exec = nullptr;
+    s->graph = nullptr;
+    s->graph_ok = false;
+}
+
+int ensure_graph(akua_pbf* s, const char* aos, size_t stride) {
+    if (s->graph_ok && s->graph_options == s->options && s->graph_aos == aos &&
+        s->graph_stride == stride)
+        return AKUA_OK;
+    invalidate_graph(s);
+    cudaError_t e = cudaStreamBeginCapture(s->capture_stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_status(e);
+    enqueue_body(s, s->capture_stream, aos, stride, false);
+    e = cudaStreamEndCapture(s->capture_stream, &s->graph);
+    if (e != cudaSuccess) {
+        s->graph = nullptr;
+        return cuda_status(e);
+    }
+    e = cudaGraphInstantiate(&s->exec, s->graph, 0);
+    if (e != cudaSuccess) {
+        s->exec = nullptr;
+        return cuda_status(e);
+    }
+    s->graph_ok = true;
+    s->graph_options = s->options;
+    s->graph_aos = aos;
+    s->graph_stride = stride;
+    ++s->graph_captures;
+    return AKUA_OK;
+}
+
+int do_step(akua_pbf* s, const char* aos, size_t stride, bool force_import, float dt,
+            const float* bmin, const float* bmax) {
+    if (!(std::isfinite(dt) && dt > 0.0f) || !finite3(bmin) || !finite3(bmax))
+        return AKUA_ERR_INVALID_ARGUMENT;
+    cudaGetLastError();  // clear a stale error of an unrelated call
+    const StepParams p = make_params(s, dt, bmin, bmax);
+    cudaStream_t st = s->stream;
+    const bool prof = s->prof_active && s->prof_steps_left > 0;
+    Marker mark{s, st, prof};
+    if (prof) {
+        --s->prof_steps_left;
+        if (s->prof_next < s->prof_events.size()) {  // step start
+            cudaEventRecord(s->prof_events[s->prof_next], st);
+            s->prof_names[s->prof_next++] = nullptr;
+        }
+    }
+    akua::k_set_params<<<1, 32, 0, st>>>(p, s->d_params);
+    mark("k_set_params");
+    const bool import = force_import || !(s->options & AKUA_PBF_OPT_RESIDENT) || !s->state_valid;
+    if (import) {
+        akua::k_import<<<grid_for(s->n, akua::kElemBlock), akua::kElemBlock, 0, st>>>(
+            aos, stride, s->n, s->x4, s->v4, s->col4, s->size, s->rho, s->lam, s->dp4,
+            s->cfg.solverIterations == 0 ? 1 : 0);
+        mark("k_import");
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_status(e);
+    if ((s->options & AKUA_PBF_OPT_NO_GRAPH) || prof) {
+        enqueue_body(s, st, aos, stride, prof);
+    } else {
+        const int rc = ensure_graph(s, aos, stride);
+        if (rc != AKUA_OK) return rc;
+        e = cudaGraphLaunch(s->exec, st);
+        if (e != cudaSuccess) return cuda_status(e);
+    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_status(e);
+    s->state_valid = true;
+    ++s->steps;
+    return AKUA_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void akua_pbf_default_config(akua_pbf_config* c, akua_lambda_corr_params* k) {
+    if (c) {
+        c->restDensity = 7600.0f;
+        c->particle_spacing = 0.05f;
+        c->smoothRadius = 0.1f;
+        c->spatialHashCellSize = 0.1f;
+        c->relaxation = 600.0f;
+        c->vorticityEpsilon = 0.00001f;
+        c->viscosity = 0.01f;
+        c->maxNeighbours = 128;
+        c->solverIterations = 4;
+        c->gravity[0] = 0.0f;
+        c->gravity[1] = -9.8f;
+        c->gravity[2] = 0.0f;
+    }
+    if (k) {
+        k->enabled = 1;
+        k->k = 0.0001f;
+        k->n = 4.0f;
+        k->delta_q = 0.03f;
+    }
+}
+
+int akua_pbf_create(int32_t n, const akua_pbf_config* cfg, const akua_lambda_corr_params* corr,
+                    akua_pbf** out) {
+    if (!out) return AKUA_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (!cfg || !corr || n <= 0) return AKUA_ERR_INVALID_ARGUMENT;
+    if (cfg->maxNeighbours <= 0 || cfg->solverIterations < 0) return AKUA_ERR_INVALID_ARGUMENT;
+    if (!(cfg->smoothRadius > 0.0f) || !(cfg->spatialHashCellSize > 0.0f) ||
+        !(cfg->restDensity > 0.0f) || !std::isfinite(cfg->smoothRadius))
+        return AKUA_ERR_INVALID_ARGUMENT;
+    // PBFSolver.cpp:15: _tableSize = maxNeighbours * numParticles, an int.
+    if ((int64_t)cfg->maxNeighbours * (int64_t)n > (int64_t)INT_MAX) return AKUA_ERR_TOO_LARGE;
+    akua_pbf* s = new (std::nothrow) akua_pbf();
+    if (!s) return AKUA_ERR_OUT_OF_MEMORY;
+    s->n = n;
+    s->cfg = *cfg;
+    s->corr = *corr;
+    s->table_size = (uint32_t)(cfg->maxNeighbours * n);
+    s->table_alloc = s->table_size;
+    cudaGetDevice(&s->device);
+    const size_t N = (size_t)n;
+    const size_t cap = (size_t)cfg->maxNeighbours;
+    const int tiles = akua::radix::num_tiles(n);
+    cudaError_t e = cudaSuccess;
+    auto chk = [&](cudaError_t r) {
+        if (e == cudaSuccess) e = r;
+    };
+    chk(dalloc(s, &s->d_params, 1));
+    chk(dalloc(s, &s->x4, N)); chk(dalloc(s, &s->v4, N)); chk(dalloc(s, &s->col4, N));
+    chk(dalloc(s, &s->x4g, N)); chk(dalloc(s, &s->v4g, N)); chk(dalloc(s, &s->col4g, N));
+    chk(dalloc(s, &s->ps0, N)); chk(dalloc(s, &s->ps1, N));
+    chk(dalloc(s, &s->dp4, N)); chk(dalloc(s, &s->dpg, N));
+    chk(dalloc(s, &s->vstar4, N)); chk(dalloc(s, &s->om4, N)); chk(dalloc(s, &s->vc4, N));
+    chk(dalloc(s, &s->size, N)); chk(dalloc(s, &s->sizeg, N));
+    chk(dalloc(s, &s->rho, N)); chk(dalloc(s, &s->lam, N));
+    chk(dalloc(s, &s->rhog, N)); chk(dalloc(s, &s->lamg, N));
+    chk(dalloc(s, &s->keys0, N)); chk(dalloc(s, &s->vals0, N));
+    chk(dalloc(s, &s->keys1, N)); chk(dalloc(s, &s->vals1, N));
+    chk(dalloc(s, &s->table, (size_t)s->table_alloc));
+    chk(dalloc(s, &s->nbr, N * cap));
+    chk(dalloc(s, &s->cnt, N));
+    chk(dalloc(s, &s->counts, (size_t)akua::radix::RADIX * tiles));
+    chk(dalloc(s, &s->flags, 1));
+    if (e == cudaSuccess) e = cudaMemset(s->table, 0xff, sizeof(uint32_t) * (size_t)s->table_alloc);
+    if (e == cudaSuccess) e = cudaMemset(s->flags, 0, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemset(s->dp4, 0, sizeof(float4) * N);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->capture_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        free_all(s);
+        delete s;
+        cudaGetLastError();
+        return cuda_status(e);
+    }
+    update_sort_layout(s);
+    *out = s;
+    return AKUA_OK;
+}
+
+int akua_pbf_destroy(akua_pbf* s) {
+    if (!s) return AKUA_ERR_INVALID_ARGUMENT;
+    DeviceGuard g(s->device);
+    int rc = cuda_status(cudaStreamSynchronize(s->stream));
+    free_all(s);
+    delete s;
+    return rc;
+}
+
+int akua_pbf_attach_particles(akua_pbf* s, void* dev, size_t stride) {
+    if (!s) return AKUA_ERR_INVALID_ARGUMENT;
+    if (dev && (stride < sizeof(akua_particle) || stride % 4 != 0 ||
+                (reinterpret_cast<uintptr_t>(dev) & 3u) != 0))
+        return AKUA_ERR_INVALID_ARGUMENT;
+    s->attached = static_cast<char*>(dev);
+    s->stride = dev ? stride : 0;
+    s->state_valid = false;
+    return AKUA_OK;
+}
+
+int akua_pbf_step(akua_pbf* s, float dt, const float bmin[3], const float bmax[3]) {
+    if (!s) return AKUA_ERR_INVALID_ARGUMENT;
+    if (!s->attached) return AKUA_ERR_NOT_ATTACHED;
+    DeviceGuard g(s->device);
+    return do_step(s, s->attached, s->stride, false, dt, bmin, bmax);
+}
+
+int akua_pbf_step_host(akua_pbf* s, void* host, size_t stride, float dt, const float bmin[3],
+                       const float bmax[3]) {
+    if (!s || !host || stride < sizeof(akua_particle) || stride % 4 != 0)
+        return AKUA_ERR_INVALID_ARGUMENT;
+    DeviceGuard g(s->device);
+    const size_t bytes = (size_t)s->n * stride;
+    if (s->staging_bytes < bytes) {
+        if (s->staging) {
+            cudaStreamSynchronize(s->stream);
+            cudaFree(s->staging);
+            s->device_bytes -= s->staging_bytes;
+            s->staging = nullptr;
+            s->staging_bytes = 0;
+        }
+        cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&s->staging), bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            s->staging = nullptr;
+            return cuda_status(e);
+        }
+        s->staging_bytes = bytes;
+        s->device_bytes += bytes;
+    }
+    cudaError_t e = cudaMemcpyAsync(s->staging, host, bytes, cudaMemcpyHostToDevice, s->stream);
+    if (e != cudaSuccess) return cuda_status(e);
+    int rc = do_step(s, s->staging, stride, true, dt, bmin, bmax);
+    if (rc != AKUA_OK) return rc;
+    e = cudaMemcpyAsync(host, s->staging, bytes, cudaMemcpyDeviceToHost, s->stream);
+    if (e != cudaSuccess) return cuda_status(e);
+    return cuda_status(cudaStreamSynchronize(s->stream));
+}
+
+int akua_pbf_set_gravity(akua_pbf* s, const float g[3]) {
+    if (!s || !finite3(g)) return AKUA_ERR_INVALID_ARGUMENT;
+    for (int a = 0; a < 3; ++a) s->cfg.gravity[a] = g[a];
+    return AKUA_OK;
+}
+
+int akua_pbf_set_boundary_damping(akua_pbf* s, float restitution, float friction) {
+    if (!s || !std::isfinite(restitution) || !std::isfinite(friction))
+        return AKUA_ERR_INVALID_ARGUMENT;
+    s->restitution = restitution;
+    s->friction = friction;
+    return AKUA_OK;
+}
+
+int akua_pbf_set_table_size(akua_pbf* s, int32_t table_size) {
+    if (!s || table_size <= 0) return AKUA_ERR_INVALID_ARGUMENT;
+    DeviceGuard g(s->device);
+    if ((uint32_t)table_size > s->table_alloc) {
+        cudaError_t e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess) return cuda_status(e);
+        uint32_t* t = nullptr;
+        e = cudaMalloc(reinterpret_cast<void**>(&t), sizeof(uint32_t) * (size_t)table_size);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return cuda_status(e);
+        }
+        cudaFree(s->table);
+        s->device_bytes -= sizeof(uint32_t) * (size_t)s->table_alloc;
+        s->device_bytes += sizeof(uint32_t) * (size_t)table_size;
+        s->table = t;
+        s->table_alloc = (uint32_t)table_size;
+    }
+    // A smaller table reuses the allocation; stale entries are rejected by the key check.
+    cudaError_t e = cudaMemsetAsync(s->table, 0xff, sizeof(uint32_t) * (size_t)s->table_alloc,
+                                    s->stream);
+    if (e != cudaSuccess) return cuda_status(e);
+    s->table_size = (uint32_t)table_size;
+    update_sort_layout(s);
+    invalidate_graph(s);
+    return AKUA_OK;
+}
+
+int akua_pbf_set_stream(akua_pbf* s, void* stream) {
+    if (!s) return AKUA_ERR_INVALID_ARGUMENT;
+    s->stream = static_cast<cudaStream_t>(stream);
+    return AKUA_OK;
+}
+
+int akua_pbf_set_options(akua_pbf* s, uint32_t options) {
+    if (!s) return AKUA_ERR_INVALID_ARGUMENT;
+    const uint32_t known = AKUA_PBF_OPT_EXACT_MATH | AKUA_PBF_OPT_RESIDENT | AKUA_PBF_OPT_NO_GRAPH;
+    if (options & ~known) return AKUA_ERR_INVALID_ARGUMENT;
+    s->options = options;
+    return AKUA_OK;
+}
+
+int akua_pbf_synchronize(akua_pbf* s) {
+    if (!s) return AKUA_ERR_INVALID_ARGUMENT;
+    DeviceGuard g(s->device);
+    return cuda_status(cudaStreamSynchronize(s->stream));
+}
+
+int akua_pbf_get_stats(akua_pbf* s, akua_pbf_stats* st) {
+    if (!s || !st) return AKUA_ERR_INVALID_ARGUMENT;
+    DeviceGuard g(s->device);
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return cuda_status(e);
+    uint32_t flags = 0;
+    e = cudaMemcpy(&flags, s->flags, sizeof(flags), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_status(e);
+    st->numParticles = s->n;
+    st->tableSize = (int32_t)s->table_size;
+    st->maxNeighbours = s->cfg.maxNeighbours;
+    st->solverIterations = s->cfg.solverIterations;
+    st->steps = s->steps;
+    st->deviceFlags = flags;
+    st->graphCaptures = s->graph_captures;
+    st->deviceBytes = s->device_bytes;
+    return AKUA_OK;
+}
+
+int akua_pbf_read_debug(akua_pbf* s, int32_t what, void* dst, size_t bytes) {
+    if (!s || !dst) return AKUA_ERR_INVALID_ARGUMENT;
+    DeviceGuard g(s->device);
+    const size_t N = (size_t)s->n;
+    const void* src = nullptr;
+    size_t need = 0;
+    switch (what) {
+        case AKUA_DEBUG_HASHES: src = s->sorted_keys; need = N * 4; break;
+        case AKUA_DEBUG_ORDER: src = s->sorted_perm; need = N * 4; break;
+        case AKUA_DEBUG_NEIGHBOUR_COUNTS: src = s->cnt; need = N * 4; break;
+        case AKUA_DEBUG_NEIGHBOURS: src = s->nbr; need = N * (size_t)s->cfg.maxNeighbours * 4; break;
+        case AKUA_DEBUG_PARTICLES: need = N * sizeof(akua_particle); break;
+        default: return AKUA_ERR_INVALID_ARGUMENT;
+    }
+    if (bytes != need) return AKUA_ERR_INVALID_ARGUMENT;
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return cuda_status(e);
+    if (what == AKUA_DEBUG_PARTICLES) {
+        char* tmp = nullptr;
+        e = cudaMalloc(reinterpret_cast<void**>(&tmp), need);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return cuda_status(e);
+        }
+        akua::k_export<<<grid_for(s->n, akua::kElemBlock), akua::kElemBlock, 0, s->stream>>>(
+            tmp, sizeof(akua_particle), s->n, s->x4, s->v4, s->vstar4, s->dp4, s->om4, s->rho,
+            s->lam, s->sorted_keys, s->col4, s->size);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dst, tmp, need, cudaMemcpyDeviceToHost, s->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        cudaFree(tmp);
+        return cuda_status(e);
+    }
+    e = cudaMemcpy(dst, src, need, cudaMemcpyDeviceToHost);
+    return cuda_status(e);
+}
+
+int akua_pbf_kernels_per_step(akua_pbf* s) {
+    if (!s) return AKUA_ERR_INVALID_ARGUMENT;
+    // parameter upload + import (when it runs) + the body
+    const bool import = !(s->options & AKUA_PBF_OPT_RESIDENT);
+    if (s->body_launches == 0) return AKUA_ERR_INVALID_ARGUMENT;  // no step issued yet
+    return 1 + (import ? 1 : 0) + s->body_launches;
+}
+
+int akua_pbf_profile_begin(akua_pbf* s, int32_t max_steps) {
+    if (!s || max_steps <= 0 || max_steps > 100000) return AKUA_ERR_INVALID_ARGUMENT;
+    DeviceGuard g(s->device);
+    for (cudaEvent_t ev : s->prof_events) cudaEventDestroy(ev);
+    s->prof_events.clear();
+    const size_t per_step = 8 + 3 * (size_t)s->passes + 2 * (size_t)s->cfg.solverIterations + 8;
+    const size_t total = per_step * (size_t)max_steps;
+    s->prof_events.resize(total, nullptr);
+    s->prof_names.assign(total, nullptr);
+    for (size_t i = 0; i < total; ++i) {
+        cudaError_t e = cudaEventCreate(&s->prof_events[i]);
+        if (e != cudaSuccess) {
+            s->prof_events.resize(i);
+            return cuda_status(e);
+        }
+    }
+    s->prof_next = 0;
+    s->prof_steps_left = max_steps;
+    s->prof_active = true;
+    return AKUA_OK;
+}
+
+int akua_pbf_profile_end(akua_pbf* s, akua_kernel_time* out, int32_t capacity, int32_t* count) {
+    if (!s || !count || (capacity > 0 && !out)) return AKUA_ERR_INVALID_ARGUMENT;
+    DeviceGuard g(s->device);
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    std::map<std::string, std::pair<int, double>> acc;
+    std::vector<std::string> order;
+    for (size_t i = 1; e == cudaSuccess && i < s->prof_next; ++i) {
+        const char* name = s->prof_names[i];
+        if (!name) continue;  // start of a step: nothing ran since the previous event
+        float ms = 0.f;
+        e = cudaEventElapsedTime(&ms, s->prof_events[i - 1], s->prof_events[i]);
+        if (e != cudaSuccess) break;
+        auto it = acc.find(name);
+        if (it == acc.end()) {
+            order.push_back(name);
+            acc[name] = {1, (double)ms};
+        } else {
+            it->second.first += 1;
+            it->second.second += ms;
+        }
+    }
+    for (cudaEvent_t ev : s->prof_events) cudaEventDestroy(ev);
+    s->prof_events.clear();
+    s->prof_names.clear();
+    s->prof_next = 0;
+    s->prof_active = false;
+    s->prof_steps_left = 0;
+    if (e != cudaSuccess) return cuda_status(e);
+    int32_t k = 0;
+    for (const std::string& name : order) {
+        if (k < capacity) {
+            std::snprintf(out[k].name, sizeof(out[k].name), "%s", name.c_str());
+            out[k].launches = acc[name].first;
+            out[k].total_ms = acc[name].second;
+        }
+        ++k;
+    }
+    *count = k;
+    return AKUA_OK;
+}
+
+const char* akua_pbf_status_string(int status) {
+    switch (status) {
+        case AKUA_OK: return "ok";
+        case AKUA_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case AKUA_ERR_CUDA: return "CUDA error";
+        case AKUA_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case AKUA_ERR_NOT_ATTACHED: return "no particle buffer attached";
+        case AKUA_ERR_DEVICE_CHECK: return "device-side check failed";
+        case AKUA_ERR_TOO_LARGE: return "size exceeds the entry point's limit";
+        default: return "unknown status";
+    }
+}
+
+int akua_pbf_abi_version(void) { return AKUA_PBF_ABI_VERSION; }
+
+}  // extern "C"

@@ -1,0 +1,345 @@
+#!/usr/bin/env python3
+"""PBF step benchmark on GB300: 1M-particle dam-break steps per second.
+
+One step = AkuaEngine's PBFSolver::step over the attached 108-byte particle records: predict, hash,
+sort, neighbour lists, 4 Jacobi iterations (density, lambda, delta with artificial pressure,
+correct + clamp), update, boundary damping, vorticity confinement, XSPH, written back into the
+records in hash order.  Workload: 100x100x100 lattice block at spacing 0.5h with seeded jitter of
++-0.01h in a box 3 x 1.5 x 1.5 block widths, dt 0.0083, seeded synthetic data.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl ours|reference]
+
+Under torchrun each rank steps its own replica of the scene (no data exchange: replicas only) and
+rank 0 prints one JSON line.  `--impl reference` times the reference algorithm's CPU restatement
+(the oracle; the reference's own code is GPU-only and cannot run on host cores) with all host
+threads, on rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import io
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "1M-particle PBF steps/s"
+UNIT = "steps/s"
+WORKLOAD = "dam_break_1m"
+
+# Algorithmic bytes per particle moved by each kernel (compulsory traffic of the SoA design;
+# neighbour positions re-read from cache are not counted, neighbour lists are).  `C` stands for
+# the mean neighbour count, filled in from the run.
+KERNEL_BYTES = {
+    "k_import": lambda c: 48 + 52,          # R x,v,m,colour,size of the record; W SoA
+    "k_predict_hash": lambda c: 24 + 4,     # R x, v; W key
+    "radix_upsweep": lambda c: 4,           # R key
+    "radix_downsweep": lambda c: 16,        # R key, value; W key, value
+    "k_gather": lambda c: 4 + 48 + 48 + 12,  # R perm, state; W state, predicted x
+    "k_build_table": lambda c: 4,           # R key
+    "k_search": lambda c: 12 + 4 + 4 * c + 4 + 8,   # R x*, key; W list, count, rho, lambda
+    "k_density_lambda": lambda c: 12 + 4 + 4 + 4 * c + 8,  # R x*, m, count, list; W rho, lambda
+    "k_delta_correct": lambda c: 12 + 4 + 4 + 4 * c + 12 + 12,  # R x*, lambda, count, list; W x*, dp
+    "k_delta_final": lambda c: 12 + 4 + 4 + 4 * c + 12 + 12 + 12 + 12 + 12,  # + R x; W x, v, v*, dp
+    "k_vorticity": lambda c: 12 + 12 + 4 + 4 * c + 12,   # R x, v, count, list; W omega
+    "k_confine": lambda c: 12 + 12 + 12 + 4 + 4 + 4 * c + 16,  # R x, v, omega, rho, count, list; W v
+    "k_xsph": lambda c: 12 + 16 + 4 + 4 * c + 12,        # R x, v+m/rho, count, list; W v
+    "k_export": lambda c: 108,              # W the record
+}
+
+
+def parse_args(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default=WORKLOAD)
+    ap.add_argument("--profile-steps", type=int, default=10)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--exact", action="store_true", help="IEEE math in pair terms")
+    return ap.parse_args(argv)
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return world, rank, local
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.out = None
+
+    def start(self):
+        try:
+            self.out = open(os.devnull if False else self._path(), "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.device)], stdout=self.out, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def _path(self):
+        d = os.path.join(ROOT, "gpurun_out") if os.path.isdir(os.path.join(ROOT, "gpurun_out")) \
+            else "/tmp"
+        return os.path.join(d, "bench_clocks_%d_%d.csv" % (self.device, os.getpid()))
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.out.close()
+        rows = []
+        with open(self._path()) as f:
+            for r in csv.reader(f):
+                if len(r) >= 9:
+                    rows.append([x.strip() for x in r])
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "", 1).isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "", 1).isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------------- oracle arm
+def time_oracle(sc, cfg, corr, steps, budget_s, threads=0):
+    """Times the CPU restatement on `steps` steps, on a sub-block when the full scene would take
+    longer than `budget_s`.  Returns (steps/s at full size, cores, sample description)."""
+    import numpy as np
+
+    import oracle
+
+    P = oracle.make_params(cfg, corr, sc.dt, sc.box_min, sc.box_max, n=sc.n, num_threads=threads)
+    cores = threads if threads > 0 else oracle.max_threads()
+    p = sc.particles.copy()
+    t0 = time.perf_counter()
+    oracle.step(p, P)
+    t1 = time.perf_counter() - t0
+    n_sample = sc.n
+    parts = p
+    if t1 * steps > budget_s:
+        frac = max(budget_s / (t1 * steps), 0.02)
+        n_sample = max(int(sc.n * frac), 4096)
+        parts = p[:n_sample].copy()  # a contiguous slab of the hash-sorted particle set
+        P = oracle.make_params(cfg, corr, sc.dt, sc.box_min, sc.box_max, n=n_sample,
+                               num_threads=threads)
+        oracle.step(parts, P)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        oracle.step(parts, P)
+    el = time.perf_counter() - t0
+    psps = n_sample * steps / el
+    sample = "%d steps of %d particles%s (%.1f s)" % (
+        steps, n_sample, "" if n_sample == sc.n else " (first particles of the sorted scene)", el)
+    return psps / sc.n, psps, cores, sample
+
+
+def run_reference(args, sc, cfg, corr):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    budget = 150.0
+    per_step_budget = budget / max(args.steps, 1)
+    # warm-up: W steps of a small sample (the oracle has no caches to warm beyond the first call)
+    sps, psps, cores, sample = time_oracle(sc, cfg, corr, args.steps, budget)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": sps, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / sps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded lattice + jitter)",
+        "config": {"workload": args.workload, "particles": sc.n, "solver_iterations": 4,
+                   "dt": sc.dt, "hardware": "host CPU cores", "per_step_budget_s": per_step_budget},
+        "cpu_baseline": {"value": sps, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": sample, "particle_steps_per_s": psps},
+        "e2e": {"value": sps, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference's step is CUDA-only; its algorithm restated on the CPU is timed",
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------------- GPU arm
+def run_ours(args, sc, cfg, corr):
+    import numpy as np
+    import torch
+
+    import akuaengine_gb300 as ak
+    from akuaengine_gb300 import PBFSolver
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    ak.load_library()
+
+    stream = torch.cuda.Stream()
+    opts = ak.OPT_EXACT_MATH if args.exact else 0
+    solver = PBFSolver(sc.n, cfg, corr, options=opts, stream=stream)
+    host = sc.particles
+    buf = torch.from_numpy(host.view(np.uint8).copy()).cuda()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            solver.step(buf, sc.dt, sc.box_min, sc.box_max)
+    torch.cuda.synchronize()
+    cnt = solver.read_debug(ak.DEBUG_NEIGHBOUR_COUNTS)
+    mean_c = float(cnt.mean())
+
+    # timed region: K steps on the solver's stream, events on that stream
+    sampler = ClockSampler(local)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    time.sleep(0.3)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        solver.step(buf, sc.dt, sc.box_min, sc.box_max)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    barrier()
+    ms = ev0.elapsed_time(ev1)
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * args.steps / (ms / 1000.0)
+    launches_per_step = solver.kernels_per_step()
+
+    # per-kernel durations (CUDA events between consecutive kernels on the same stream)
+    solver.profile_begin(args.profile_steps)
+    for _ in range(args.profile_steps):
+        solver.step(buf, sc.dt, sc.box_min, sc.box_max)
+    prof = solver.profile_end()
+    total = sum(v[1] for v in prof.values())
+    kernels = {k: {"launches": v[0], "ms_total": round(v[1], 4),
+                   "us_per_launch": round(1000.0 * v[1] / max(v[0], 1), 2),
+                   "share": round(v[1] / total, 4)} for k, v in prof.items()}
+    dom = max((k for k in prof if k in KERNEL_BYTES), key=lambda k: prof[k][1])
+    per_launch_s = prof[dom][1] / prof[dom][0] / 1000.0
+    alg_bytes = KERNEL_BYTES[dom](mean_c) * sc.n
+    peak, peak_kind = load_peaks()
+    achieved = alg_bytes / per_launch_s / 1e9
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            tr = json.load(f)
+        if dom in tr.get("bytes_per_launch", {}) and tr.get("workload") == args.workload:
+            traffic = tr["bytes_per_launch"][dom]
+    except Exception:
+        pass
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
+                "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                "traffic": traffic, "algorithmic_bytes": alg_bytes,
+                "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_kind
+                if peak_kind == "measured" else "fallback 6.8 TB/s"}
+
+    # end to end through the public API: pinned host records -> device, step, -> host
+    e2e = None
+    if not args.no_e2e:
+        pinned = torch.empty(host.nbytes, dtype=torch.uint8, pin_memory=True)
+        pinned.numpy()[:] = host.view(np.uint8)
+        hp = pinned.numpy().view(ak.PARTICLE_DTYPE)
+        for _ in range(2):
+            solver.step_host(hp, sc.dt, sc.box_min, sc.box_max)
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            solver.step_host(hp, sc.dt, sc.box_min, sc.box_max)
+        el = time.perf_counter() - t0
+        if dist is not None:
+            t = torch.tensor([el], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            el = float(t.item())
+        e2e = {"value": world * args.steps / el, "unit": UNIT,
+               "h2d_bytes_per_step": int(host.nbytes), "d2h_bytes_per_step": int(host.nbytes),
+               "api": "akua_pbf_step_host (pinned host records)"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sps, psps, cores, sample = time_oracle(sc, cfg, corr, 3, 30.0)
+        cpu = {"value": sps, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+               "particle_steps_per_s": psps}
+
+    solver.close()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded lattice block + uniform jitter 0.01h)",
+            "config": {"workload": args.workload, "particles": sc.n, "block": [100, 100, 100],
+                       "box_block_widths": [3.0, 1.5, 1.5], "dt": sc.dt, "solver_iterations": 4,
+                       "max_neighbours": cfg.maxNeighbours, "table_size": cfg.maxNeighbours * sc.n,
+                       "corr": {"k": corr.k, "n": corr.n, "delta_q": corr.delta_q},
+                       "math": "exact" if args.exact else "fast",
+                       "parallelism": "replicas x%d" % world,
+                       "l2": "per-step working set > L2 (no flush)",
+                       "mean_neighbours": round(mean_c, 3)},
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": launches_per_step * args.steps,
+            "clocks": clocks,
+            "kernels": kernels,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main(argv=None):
+    args = parse_args(argv)
+    from akuaengine_gb300 import scene
+
+    sc = scene.workload(args.workload, seed=0)
+    cfg, corr = scene.benchmark_params()
+    if args.impl == "reference":
+        run_reference(args, sc, cfg, corr)
+    else:
+        run_ours(args, sc, cfg, corr)
+
+
+if __name__ == "__main__":
+    main()

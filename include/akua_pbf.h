@@ -1,0 +1,177 @@
+/*
+ * akua_pbf.h — C ABI of the GB300 Position-Based Fluids step.
+ *
+ * Drop-in for AkuaEngine's per-frame solver step.  Each entry point names the reference
+ * interface it replaces (paths relative to the AkuaEngine source tree).  Plain pointers and sizes
+ * only; every call returns a status (0 = ok, negative = error) — the reference reports no errors.
+ *
+ * Threading: a handle is not thread-safe.  All device work of a handle is issued on one CUDA
+ * stream (the legacy default stream unless akua_pbf_set_stream is called) and is asynchronous
+ * with respect to the host unless stated otherwise.
+ */
+#ifndef AKUA_PBF_H
+#define AKUA_PBF_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AKUA_PBF_ABI_VERSION 1
+
+/* Status codes. */
+#define AKUA_OK 0
+#define AKUA_ERR_INVALID_ARGUMENT (-1)
+#define AKUA_ERR_CUDA (-2)
+#define AKUA_ERR_OUT_OF_MEMORY (-3)
+#define AKUA_ERR_NOT_ATTACHED (-4)  /* step before a particle buffer was attached */
+#define AKUA_ERR_DEVICE_CHECK (-5)  /* a device-side consistency check failed */
+#define AKUA_ERR_TOO_LARGE (-6)     /* a size exceeds a fixed limit of the called entry point */
+
+/* Options (akua_pbf_set_options). */
+#define AKUA_PBF_OPT_EXACT_MATH 0x1u /* IEEE sqrt/divide in every pair term (bit-reproducible) */
+#define AKUA_PBF_OPT_RESIDENT 0x2u   /* read the attached buffer only on the first step */
+#define AKUA_PBF_OPT_NO_GRAPH 0x4u   /* launch kernels one by one instead of a captured graph */
+
+/* Solver parameters: AkuaEngine::PBFConfig, include/AkuaEngine/Simulation/PBFConfig.h:18-29. */
+typedef struct akua_pbf_config {
+    float restDensity;
+    float particle_spacing;     /* carried; the step does not read it (as in the reference) */
+    float smoothRadius;         /* kernel radius h; also the hashing cell (NeighbourSearchCUDA.cu:163) */
+    float spatialHashCellSize;  /* cell used by the neighbour walk (NeighbourSearchCUDA.cu:177) */
+    float relaxation;           /* epsilon in the lambda denominator */
+    float vorticityEpsilon;
+    float viscosity;            /* XSPH coefficient c */
+    int32_t maxNeighbours;      /* list capacity per particle; table size = maxNeighbours * N */
+    int32_t solverIterations;
+    float gravity[3];
+} akua_pbf_config;
+
+/* Artificial pressure: AkuaEngine::LambdaCorrParams, PBFConfig.h:10-15. */
+typedef struct akua_lambda_corr_params {
+    int32_t enabled; /* carried; never read, as in the reference */
+    float k;
+    float n;
+    float delta_q;
+} akua_lambda_corr_params;
+
+/* One particle record: AkuaEngine::Particle, include/AkuaEngine/Simulation/Particle.h:8-31
+ * (108 bytes, 4-byte aligned).  This is also the vertex layout the reference renders from. */
+typedef struct akua_particle {
+    float position[3];
+    float velocity[3];
+    float new_position[3];
+    float new_velocity[3];
+    float position_delta[3];
+    float vorticity[3];
+    float mass;
+    float density;
+    float lambda;
+    uint32_t hash;
+    float color[4];
+    float size;
+} akua_particle;
+
+typedef struct akua_pbf akua_pbf;
+
+/* Per-handle counters (akua_pbf_get_stats). */
+typedef struct akua_pbf_stats {
+    int32_t numParticles;
+    int32_t tableSize;
+    int32_t maxNeighbours;
+    int32_t solverIterations;
+    int64_t steps;            /* steps issued on this handle */
+    uint32_t deviceFlags;     /* bit 0: some list reached maxNeighbours; bit 1: bad table entry */
+    int32_t graphCaptures;    /* how many times the step graph was (re)captured */
+    uint64_t deviceBytes;     /* device memory held by the handle */
+} akua_pbf_stats;
+
+/* Debug readbacks (akua_pbf_read_debug), all for the sorted order of the last step. */
+#define AKUA_DEBUG_HASHES 1           /* uint32[N]: cell hash per particle */
+#define AKUA_DEBUG_ORDER 2            /* uint32[N]: pre-sort index of the particle now at slot s */
+#define AKUA_DEBUG_NEIGHBOUR_COUNTS 3 /* uint32[N] */
+#define AKUA_DEBUG_NEIGHBOURS 4       /* uint32[N * maxNeighbours], row i holds particle i's list */
+#define AKUA_DEBUG_PARTICLES 5        /* akua_particle[N]: the solver's current state */
+
+/* Reference defaults of PBFConfig / LambdaCorrParams (PBFConfig.h:10-29). */
+void akua_pbf_default_config(akua_pbf_config* config, akua_lambda_corr_params* corr);
+
+/* Replaces PBFSolver::PBFSolver(int, const PBFConfig&, const LambdaCorrParams&)
+ * (src/Simulation/PBFSolver.cpp:13-20).  Allocates all device memory of the handle on the
+ * current device: the neighbour lists (N * maxNeighbours), the cell table (maxNeighbours * N
+ * entries, PBFSolver.cpp:15) and the SoA particle state. */
+int akua_pbf_create(int32_t numParticles, const akua_pbf_config* config,
+                    const akua_lambda_corr_params* corr, akua_pbf** out);
+
+/* Frees the handle and its device memory (synchronises the handle's stream first). */
+int akua_pbf_destroy(akua_pbf* solver);
+
+/* Replaces InteropResource + cudaGraphicsResourceGetMappedPointer (src/Interop/InteropResource.cpp:9-14,
+ * src/CUDA/IntegrationCUDA.cu:201-204): `deviceParticles` is a device array of N particle records
+ * with `strideBytes` between records (108 for akua_particle; larger strides are allowed, must be a
+ * multiple of 4).  The solver reads and rewrites the records in place, leaving them sorted by cell
+ * hash as the reference does.  Pass NULL to detach. */
+int akua_pbf_attach_particles(akua_pbf* solver, void* deviceParticles, size_t strideBytes);
+
+/* Replaces PBFSolver::step(const InteropResource&, float, glm::vec3, glm::vec3)
+ * (src/Simulation/PBFSolver.cpp:22-78): predict, hash, sort, neighbour lists, solverIterations
+ * Jacobi iterations of the density constraint, update, boundary damping, vorticity confinement and
+ * XSPH viscosity over the attached buffer.  Asynchronous on the handle's stream. */
+int akua_pbf_step(akua_pbf* solver, float deltaTime, const float boxMin[3], const float boxMax[3]);
+
+/* The same step for callers that hold the particle array in host memory: copies the N records
+ * to the device, steps, and copies them back (stride as in akua_pbf_attach_particles).
+ * Synchronous: returns after the records are back in `hostParticles`. */
+int akua_pbf_step_host(akua_pbf* solver, void* hostParticles, size_t strideBytes, float deltaTime,
+                       const float boxMin[3], const float boxMax[3]);
+
+/* Replaces PBFSolver::setGravity(glm::vec3) (include/AkuaEngine/Simulation/PBFSolver.h:29-31). */
+int akua_pbf_set_gravity(akua_pbf* solver, const float gravity[3]);
+
+/* Boundary velocity damping coefficients; the reference hard-codes restitution 0 and friction 0.95
+ * at its call site (src/Simulation/PBFSolver.cpp:64), which are the defaults here. */
+int akua_pbf_set_boundary_damping(akua_pbf* solver, float restitution, float friction);
+
+/* Cell table size; the reference fixes it to maxNeighbours * N (PBFSolver.cpp:15), the default.
+ * Changing it changes every hash, hence the sorted order. */
+int akua_pbf_set_table_size(akua_pbf* solver, int32_t tableSize);
+
+/* New: the CUDA stream (a cudaStream_t) all device work of this handle is issued on. */
+int akua_pbf_set_stream(akua_pbf* solver, void* cudaStream);
+
+/* New: AKUA_PBF_OPT_* flags. */
+int akua_pbf_set_options(akua_pbf* solver, uint32_t options);
+
+/* New: blocks until the handle's device work is done; reports deferred device errors. */
+int akua_pbf_synchronize(akua_pbf* solver);
+
+/* New: counters; synchronises the handle's stream. */
+int akua_pbf_get_stats(akua_pbf* solver, akua_pbf_stats* stats);
+
+/* New: copies one AKUA_DEBUG_* array to host memory (synchronous); `bytes` must match. */
+int akua_pbf_read_debug(akua_pbf* solver, int32_t what, void* hostDst, size_t bytes);
+
+/* New: how many of the library's kernels one akua_pbf_step launches with the current settings. */
+int akua_pbf_kernels_per_step(akua_pbf* solver);
+
+/* New: per-kernel timing of the next steps with CUDA events recorded on the handle's stream
+ * between consecutive kernels.  While profiling, steps are launched kernel by kernel (no graph). */
+typedef struct akua_kernel_time {
+    char name[40];
+    int32_t launches;
+    double total_ms;
+} akua_kernel_time;
+int akua_pbf_profile_begin(akua_pbf* solver, int32_t maxSteps);
+/* Ends profiling; synchronises; writes up to `capacity` entries (one per kernel name). */
+int akua_pbf_profile_end(akua_pbf* solver, akua_kernel_time* out, int32_t capacity, int32_t* count);
+
+const char* akua_pbf_status_string(int status);
+int akua_pbf_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AKUA_PBF_H */

@@ -1,0 +1,323 @@
+"""GPU parity: the CUDA step (through the C ABI) against the CPU oracle on the same seeded inputs.
+
+Bars:
+  * cell hashes, sorted order, neighbour lists and counts: bit-exact, in both math modes;
+  * AKUA_PBF_OPT_EXACT_MATH: every field of every record bit-exact, over many steps;
+  * default (fast) math: floats within the tolerances written in each test.
+"""
+import numpy as np
+import pytest
+
+import oracle
+import akuaengine_gb300 as ak
+from akuaengine_gb300 import LambdaCorrParams, PBFConfig, PBFSolver, scene
+
+pytestmark = pytest.mark.gpu
+
+FLOAT_FIELDS = ["position", "velocity", "new_position", "new_velocity", "position_delta",
+                "vorticity", "mass", "density", "lambda", "color", "size"]
+
+
+def bench_params():
+    """Benchmark workloads' parameters: reference scene values, dt 0.0083, reference
+    artificial pressure (k=1e-4, n=4, dq=0.03)."""
+    return PBFConfig(), LambdaCorrParams()
+
+
+def strong_corr():
+    """The artificial pressure k=0.1, n=4, dq=0.2h; with the reference's rho0 and mass it makes
+    the fluid break apart, which exercises sparse neighbourhoods."""
+    return LambdaCorrParams(k=0.1, n=4.0, delta_q=0.02)
+
+
+def run_gpu(sc, cfg, corr, steps=1, options=0, table_size=None, particles=None):
+    p = (sc.particles if particles is None else particles).copy()
+    with PBFSolver(sc.n, cfg, corr, options=options, table_size=table_size) as s:
+        for _ in range(steps):
+            s.step_host(p, sc.dt, sc.box_min, sc.box_max)
+        extra = {
+            "order": s.read_debug(ak.DEBUG_ORDER),
+            "hashes": s.read_debug(ak.DEBUG_HASHES),
+            "cnt": s.read_debug(ak.DEBUG_NEIGHBOUR_COUNTS),
+            "nbr": s.read_debug(ak.DEBUG_NEIGHBOURS),
+            "stats": s.stats(),
+        }
+    return p, extra
+
+
+def run_oracle(sc, cfg, corr, steps=1, flags=oracle.FMA, table_size=None, particles=None):
+    p = (sc.particles if particles is None else particles).copy()
+    P = oracle.make_params(cfg, corr, sc.dt, sc.box_min, sc.box_max, n=sc.n, flags=flags,
+                           table_size=table_size)
+    out = None
+    for k in range(steps):
+        out = oracle.step(p, P, want_lists=(k == steps - 1))
+    perm, nbr, cnt = out
+    return p, {"order": perm, "nbr": nbr, "cnt": cnt}
+
+
+def assert_grid_equal(g, o, cap):
+    assert np.array_equal(g["order"], o["order"]), "sorted order differs"
+    assert np.array_equal(g["cnt"], o["cnt"]), "neighbour counts differ"
+    n = len(g["cnt"])
+    mask = np.arange(cap)[None, :] < g["cnt"][:, None]
+    assert np.array_equal(np.where(mask, g["nbr"], 0), np.where(mask, o["nbr"], 0)), \
+        "neighbour lists differ"
+
+
+def assert_records_bitexact(a, b):
+    for f in FLOAT_FIELDS + ["hash"]:
+        x, y = a[f], b[f]
+        if not np.array_equal(x.view(np.uint32), y.view(np.uint32)):
+            bad = np.argwhere(x.view(np.uint32) != y.view(np.uint32))
+            raise AssertionError("%s differs at %d places, first %s: %r vs %r"
+                                 % (f, len(bad), bad[0], x[tuple(bad[0])], y[tuple(bad[0])]))
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib(cuda_lib):
+    return cuda_lib
+
+
+# --- exact math: bit-exact records -----------------------------------------------------------
+
+def test_exact_one_step_27k_bitexact():
+    sc = scene.workload("dam_break_27k", seed=0)
+    cfg, corr = bench_params()
+    g, ge = run_gpu(sc, cfg, corr, 1, ak.OPT_EXACT_MATH)
+    o, oe = run_oracle(sc, cfg, corr, 1)
+    assert np.array_equal(ge["hashes"], o["hash"])
+    assert_grid_equal(ge, oe, cfg.maxNeighbours)
+    assert_records_bitexact(g, o)
+
+
+@pytest.mark.parametrize("strong", [False, True])
+def test_exact_many_steps_bitexact(strong):
+    sc = scene.dam_break((14, 12, 10), (3.0, 3.0, 3.0), seed=7)
+    cfg = PBFConfig()
+    corr = strong_corr() if strong else LambdaCorrParams()
+    g, ge = run_gpu(sc, cfg, corr, 25, ak.OPT_EXACT_MATH)
+    o, oe = run_oracle(sc, cfg, corr, 25)
+    assert_grid_equal(ge, oe, cfg.maxNeighbours)
+    assert_records_bitexact(g, o)
+
+
+def test_exact_reference_scene_bitexact():
+    """The reference's own scene (Application.cpp:162-192, no jitter, dt 0.016, default corr)."""
+    sc = scene.reference_dam_break()
+    cfg, corr = PBFConfig(), LambdaCorrParams()
+    g, ge = run_gpu(sc, cfg, corr, 5, ak.OPT_EXACT_MATH)
+    o, oe = run_oracle(sc, cfg, corr, 5)
+    assert_grid_equal(ge, oe, cfg.maxNeighbours)
+    assert_records_bitexact(g, o)
+
+
+def test_capacity_truncation_bitexact():
+    sc = scene.dam_break((12, 12, 12), (3.0, 3.0, 3.0), seed=2)
+    cfg = PBFConfig(maxNeighbours=12)
+    corr = LambdaCorrParams()
+    g, ge = run_gpu(sc, cfg, corr, 3, ak.OPT_EXACT_MATH)
+    o, oe = run_oracle(sc, cfg, corr, 3)
+    assert ge["cnt"].max() == 12
+    assert ge["stats"]["deviceFlags"] & ak.FLAG_CAP_REACHED
+    assert_grid_equal(ge, oe, cfg.maxNeighbours)
+    assert_records_bitexact(g, o)
+
+
+def test_small_table_collisions_bitexact():
+    """A 4096-entry table makes many cells share a bucket (duplicated and foreign candidates)."""
+    sc = scene.dam_break((12, 12, 12), (3.0, 3.0, 3.0), seed=4)
+    cfg, corr = PBFConfig(), LambdaCorrParams()
+    g, ge = run_gpu(sc, cfg, corr, 3, ak.OPT_EXACT_MATH, table_size=4096)
+    o, oe = run_oracle(sc, cfg, corr, 3, table_size=4096)
+    dup = sum(len(set(oe["nbr"][i, : oe["cnt"][i]])) != oe["cnt"][i] for i in range(sc.n))
+    assert dup > 0
+    assert_grid_equal(ge, oe, cfg.maxNeighbours)
+    assert_records_bitexact(g, o)
+
+
+def test_zero_iterations_bitexact():
+    sc = scene.dam_break((8, 8, 8), (3.0, 3.0, 3.0), seed=9)
+    p = sc.particles.copy()
+    p["density"] = np.linspace(7000, 8000, sc.n, dtype=np.float32)
+    p["lambda"] = np.linspace(-1e-4, 1e-4, sc.n, dtype=np.float32)
+    p["position_delta"] = 1e-3
+    cfg, corr = PBFConfig(solverIterations=0), LambdaCorrParams()
+    g, ge = run_gpu(sc, cfg, corr, 2, ak.OPT_EXACT_MATH, particles=p)
+    o, oe = run_oracle(sc, cfg, corr, 2, particles=p)
+    assert_grid_equal(ge, oe, cfg.maxNeighbours)
+    assert_records_bitexact(g, o)
+
+
+@pytest.mark.parametrize("n", [1, 2, 7])
+def test_tiny_particle_counts(n):
+    sc = scene.dam_break((30, 30, 30), seed=1)
+    sc.particles = sc.particles[:n].copy()
+    cfg, corr = PBFConfig(), LambdaCorrParams()
+    g, ge = run_gpu(sc, cfg, corr, 3, ak.OPT_EXACT_MATH)
+    o, oe = run_oracle(sc, cfg, corr, 3)
+    assert_grid_equal(ge, oe, cfg.maxNeighbours)
+    assert_records_bitexact(g, o)
+
+
+def test_particles_outside_box_clamped_and_damped_bitexact():
+    sc = scene.dam_break((10, 10, 10), (2.0, 2.0, 2.0), seed=5)
+    p = sc.particles.copy()
+    rng = np.random.default_rng(0)
+    p["velocity"] = rng.normal(0, 3, size=(sc.n, 3)).astype(np.float32)
+    p["position"][:50] -= 0.2           # some start outside the lower walls
+    cfg, corr = PBFConfig(), strong_corr()
+    g, ge = run_gpu(sc, cfg, corr, 4, ak.OPT_EXACT_MATH, particles=p)
+    o, oe = run_oracle(sc, cfg, corr, 4, particles=p)
+    assert_grid_equal(ge, oe, cfg.maxNeighbours)
+    assert_records_bitexact(g, o)
+
+
+# --- fast math: exact grid, floats within tolerance ------------------------------------------
+
+# Tolerances of the default math against the oracle after one step from the same state.  The
+# fast path replaces IEEE sqrt/divide in pair terms by rsqrt-based forms (a few ulp each); the
+# four Jacobi iterations carry those differences into positions.
+POS_ATOL = 2e-5        # position units (boxes are 6-15 units wide)
+VEL_ATOL = 4e-3        # = POS_ATOL / dt plus XSPH/vorticity terms
+RHO_RTOL = 2e-5
+LAM_ATOL = 2e-8        # lambda magnitudes are ~1e-4
+VORT_ATOL = 5e-3
+
+
+def assert_close_fast(g, o):
+    assert np.array_equal(g["hash"], o["hash"])
+    assert np.array_equal(g["mass"], o["mass"]) and np.array_equal(g["color"], o["color"])
+    err = {
+        "position": np.abs(g["position"] - o["position"]).max(),
+        "velocity": np.abs(g["velocity"] - o["velocity"]).max(),
+        "new_velocity": np.abs(g["new_velocity"] - o["new_velocity"]).max(),
+        "density": (np.abs(g["density"] - o["density"]) / np.abs(o["density"])).max(),
+        "lambda": np.abs(g["lambda"] - o["lambda"]).max(),
+        "vorticity": np.abs(g["vorticity"] - o["vorticity"]).max(),
+    }
+    print("fast-vs-oracle max errors:", {k: float(v) for k, v in err.items()})
+    assert err["position"] <= POS_ATOL
+    assert err["velocity"] <= VEL_ATOL and err["new_velocity"] <= VEL_ATOL
+    assert err["density"] <= RHO_RTOL
+    assert err["lambda"] <= LAM_ATOL
+    assert err["vorticity"] <= VORT_ATOL
+
+
+def test_fast_one_step_27k():
+    sc = scene.workload("dam_break_27k", seed=1)
+    cfg, corr = bench_params()
+    g, ge = run_gpu(sc, cfg, corr, 1, 0)
+    o, oe = run_oracle(sc, cfg, corr, 1)
+    assert_grid_equal(ge, oe, cfg.maxNeighbours)
+    assert_close_fast(g, o)
+
+
+def test_fast_one_step_from_evolved_state():
+    """Parity from a state 40 steps into the dam break (splashes, compressed regions)."""
+    sc = scene.workload("dam_break_27k", seed=2)
+    cfg, corr = bench_params()
+    start, _ = run_oracle(sc, cfg, corr, 40)
+    g, ge = run_gpu(sc, cfg, corr, 1, 0, particles=start)
+    o, oe = run_oracle(sc, cfg, corr, 1, particles=start)
+    assert_grid_equal(ge, oe, cfg.maxNeighbours)
+    assert_close_fast(g, o)
+
+
+def test_fast_one_step_1m_full_size():
+    """The 1M-particle benchmark workload: grid bit-exact, floats within tolerance."""
+    sc = scene.workload("dam_break_1m", seed=0)
+    cfg, corr = bench_params()
+    g, ge = run_gpu(sc, cfg, corr, 1, 0)
+    o, oe = run_oracle(sc, cfg, corr, 1)
+    assert_grid_equal(ge, oe, cfg.maxNeighbours)
+    assert_close_fast(g, o)
+
+
+def test_fast_error_against_fp64_oracle():
+    """FP32 error of one GPU step measured against the same equations in double precision."""
+    sc = scene.workload("dam_break_27k", seed=3)
+    cfg, corr = bench_params()
+    g, _ = run_gpu(sc, cfg, corr, 1, 0)
+    d, _ = run_oracle(sc, cfg, corr, 1, flags=oracle.FMA | oracle.FP64)
+    f, _ = run_oracle(sc, cfg, corr, 1)
+    e_gpu = np.abs(g["position"].astype(np.float64) - d["position"]).max()
+    e_f32 = np.abs(f["position"].astype(np.float64) - d["position"]).max()
+    print("position error vs fp64: gpu fast %.3g, fp32 oracle %.3g" % (e_gpu, e_f32))
+    assert e_gpu <= 4 * e_f32 + 1e-6
+
+
+# --- host logic of the step: graph, resident state, device buffers ---------------------------
+
+def test_graph_and_direct_launch_identical():
+    sc = scene.dam_break((16, 16, 16), (3.0, 3.0, 3.0), seed=11)
+    cfg, corr = bench_params()
+    a, _ = run_gpu(sc, cfg, corr, 5, 0)
+    b, _ = run_gpu(sc, cfg, corr, 5, ak.OPT_NO_GRAPH)
+    assert a.tobytes() == b.tobytes()
+
+
+def test_resident_mode_matches_reimport():
+    torch = pytest.importorskip("torch")
+    sc = scene.dam_break((16, 16, 16), (3.0, 3.0, 3.0), seed=12)
+    cfg, corr = bench_params()
+    outs = []
+    for opts in (0, ak.OPT_RESIDENT):
+        buf = torch.from_numpy(sc.particles.view(np.uint8).copy()).cuda()
+        with PBFSolver(sc.n, cfg, corr, options=opts) as s:
+            for _ in range(6):
+                s.step(buf, sc.dt, sc.box_min, sc.box_max)
+            s.synchronize()
+        outs.append(buf.cpu().numpy().tobytes())
+    assert outs[0] == outs[1]
+
+
+def test_device_attach_matches_host_step_and_reports_launches():
+    torch = pytest.importorskip("torch")
+    sc = scene.dam_break((16, 16, 16), (3.0, 3.0, 3.0), seed=13)
+    cfg, corr = bench_params()
+    host, _ = run_gpu(sc, cfg, corr, 3, 0)
+    buf = torch.from_numpy(sc.particles.view(np.uint8).copy()).cuda()
+    with PBFSolver(sc.n, cfg, corr) as s:
+        s.set_stream(torch.cuda.current_stream())
+        for _ in range(3):
+            s.step(buf, sc.dt, sc.box_min, sc.box_max)
+        s.synchronize()
+        assert s.kernels_per_step() >= 20
+        st = s.stats()
+        assert st["steps"] == 3 and st["graphCaptures"] == 1
+    dev = buf.cpu().numpy().view(ak.PARTICLE_DTYPE)
+    assert dev.tobytes() == host.tobytes()
+
+
+def test_set_gravity_changes_step_without_recapture():
+    sc = scene.dam_break((10, 10, 10), (3.0, 3.0, 3.0), seed=14)
+    cfg, corr = bench_params()
+    p = sc.particles.copy()
+    with PBFSolver(sc.n, cfg, corr, options=ak.OPT_EXACT_MATH) as s:
+        s.step_host(p, sc.dt, sc.box_min, sc.box_max)
+        s.setGravity((0.0, 0.0, -9.8))
+        s.step_host(p, sc.dt, sc.box_min, sc.box_max)
+        assert s.stats()["graphCaptures"] == 1
+    q = sc.particles.copy()
+    cfg1 = PBFConfig()
+    P = oracle.make_params(cfg1, corr, sc.dt, sc.box_min, sc.box_max, n=sc.n)
+    oracle.step(q, P)
+    cfg2 = PBFConfig(gravity=(0.0, 0.0, -9.8))
+    P = oracle.make_params(cfg2, corr, sc.dt, sc.box_min, sc.box_max, n=sc.n)
+    oracle.step(q, P)
+    assert_records_bitexact(p, q)
+
+
+def test_errors_are_reported():
+    sc = scene.dam_break((4, 4, 4), seed=0)
+    with PBFSolver(sc.n) as s:
+        with pytest.raises(ak.AkuaError) as ei:
+            s._lib and ak._abi.check(
+                s._lib.akua_pbf_step(s._h, 0.01, ak._abi.vec3((0, 0, 0)), ak._abi.vec3((1, 1, 1))),
+                "step")
+        assert ei.value.status == ak.AKUA_ERR_NOT_ATTACHED
+        with pytest.raises(ak.AkuaError):
+            s.step_host(sc.particles.copy(), -1.0, sc.box_min, sc.box_max)
+        with pytest.raises(ak.AkuaError):
+            s.set_options(0x80)
