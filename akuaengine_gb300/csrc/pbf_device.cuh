@@ -44,6 +44,10 @@ struct StepParams {
     int32_t n;
     int32_t cap;
     uint32_t table_size;
+    uint64_t table_magic;   // floor((2^64 - 1) / table_size) + 1, for the exact u32 modulo
+    // Morton key of the walk cell: cell - sp_origin per axis, clamped to sp_bits bits
+    int32_t sp_origin[3];
+    int32_t sp_bits;
 };
 
 __device__ __forceinline__ float fmaf_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
@@ -65,12 +69,21 @@ __device__ __forceinline__ int cell_coord(float x, float cell) {
     return static_cast<int>(floorf(__fdiv_rn(x, cell)));
 }
 
+// a % d for any u32 a and d >= 1, with magic = floor((2^64 - 1) / d) + 1 (Lemire, Kaser and Kurz,
+// "Faster remainder by direct computation", 2019): the low 64 bits of magic * a hold the
+// fractional part of a / d, and its product with d carries the remainder in the high word.
+__device__ __forceinline__ uint32_t fast_mod(uint32_t a, uint64_t magic, uint32_t d) {
+    const uint64_t low = magic * (uint64_t)a;
+    return (uint32_t)__umul64hi(low, (uint64_t)d);
+}
+
 // NeighbourSearchCUDA.cu:23-27: int products wrap, u32 xor, then % tableSize as u32.
-__device__ __forceinline__ uint32_t cell_hash(int cx, int cy, int cz, uint32_t table) {
+__device__ __forceinline__ uint32_t cell_hash(int cx, int cy, int cz, uint32_t table,
+                                              uint64_t magic) {
     const uint32_t hx = static_cast<uint32_t>(cx) * 73856093u;
     const uint32_t hy = static_cast<uint32_t>(cy) * 19349663u;
     const uint32_t hz = static_cast<uint32_t>(cz) * 83492791u;
-    return (hx ^ hy ^ hz) % table;
+    return fast_mod(hx ^ hy ^ hz, magic, table);
 }
 
 // poly6 (SmoothingKernelsCUDA.h:16-21): 0 when r2 > h2, else kp * (h2 - r2)^3.

@@ -1,13 +1,16 @@
 // Host side of the GB300 PBF step: device memory, the per-step launch sequence, CUDA-graph
 // capture and the C ABI declared in include/akua_pbf.h.
 //
-// One handle = one particle set on one device.  A step is: [params] [import] then the captured
-// body: predict+hash -> radix sort -> gather -> bucket table -> neighbour walk (+ iteration 1
+// One handle = one particle set on one device.  A step is [params] [import] and then the captured
+// body: keys -> radix sort by (hash, previous reference rank) -> radix sort by Morton cell ->
+// gather into the new internal order -> reference-order tables -> neighbour walk (+ iteration 1
 // density/lambda) -> (delta+correct, density+lambda) x iterations -> delta+update+damping ->
-// vorticity -> confinement -> XSPH -> export.  Nothing on this path copies to the host or
-// synchronises; the reference instead synchronises after every kernel and moves the neighbour
-// lists through host memory four times per step (PBFSolver.h:23-24, NeighbourSearchCUDA.cu:151-154,
-// 182-183, ConstraintSolverCUDA.cu:195-198, IntegrationCUDA.cu:269-272).
+// vorticity -> confinement -> XSPH -> export in reference order.  Nothing on this path copies to
+// the host or synchronises; the reference instead synchronises after every kernel and moves the
+// neighbour lists through host memory four times per step (PBFSolver.h:23-24,
+// NeighbourSearchCUDA.cu:151-154, 182-183, ConstraintSolverCUDA.cu:195-198,
+// IntegrationCUDA.cu:269-272).
+#include <algorithm>
 #include <climits>
 #include <cmath>
 #include <cstdio>
@@ -38,20 +41,31 @@ struct akua_pbf {
     char* attached = nullptr;
     size_t stride = 0;
     bool state_valid = false;  // device state holds the particles (resident mode)
+    bool stepped = false;      // the reference-order tables describe the current state
 
     StepParams* d_params = nullptr;
+    // state, internal order
     float4 *x4 = nullptr, *v4 = nullptr, *col4 = nullptr;
-    float4 *x4g = nullptr, *v4g = nullptr, *col4g = nullptr;
-    float4 *ps0 = nullptr, *ps1 = nullptr, *dp4 = nullptr, *dpg = nullptr;
-    float4 *vstar4 = nullptr, *om4 = nullptr, *vc4 = nullptr;
-    float *size = nullptr, *sizeg = nullptr, *rho = nullptr, *lam = nullptr;
-    float *rhog = nullptr, *lamg = nullptr;
-    uint32_t *keys0 = nullptr, *vals0 = nullptr, *keys1 = nullptr, *vals1 = nullptr;
-    uint32_t *table = nullptr, *nbr = nullptr, *cnt = nullptr, *counts = nullptr, *flags = nullptr;
-    uint32_t *sorted_keys = nullptr, *sorted_perm = nullptr;
-    int passes = 0;
+    float* size = nullptr;
+    uint32_t* rref = nullptr;
+    float *rho = nullptr, *lam = nullptr;
+    float4* dp4 = nullptr;
+    // gathered copies and per-step arrays
+    float4 *x4g = nullptr, *col4g = nullptr, *ps0 = nullptr, *ps1 = nullptr;
+    float4 *vstar4 = nullptr, *om4 = nullptr, *vc4 = nullptr, *dpg = nullptr, *xref = nullptr;
+    float *sizeg = nullptr, *rhog = nullptr, *lamg = nullptr;
+    uint32_t *rrefg = nullptr, *inv = nullptr, *r2i = nullptr, *blen = nullptr, *order = nullptr;
+    // sorts: reference order (A) and Morton order (B)
+    uint32_t *ka0 = nullptr, *va0 = nullptr, *ka1 = nullptr, *va1 = nullptr;
+    uint32_t *kb0 = nullptr, *vb0 = nullptr, *kb1 = nullptr, *vb1 = nullptr;
+    uint32_t* sort_scratch = nullptr;
+    uint32_t *table = nullptr, *nbr = nullptr, *cnt = nullptr, *flags = nullptr;
     char* staging = nullptr;
     size_t staging_bytes = 0;
+
+    akua::radix::Plan plan_ref, plan_sp;
+    int sp_bits = 0;
+    uint32_t *kr = nullptr, *refperm = nullptr, *spperm = nullptr;  // sort results (set at enqueue)
 
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -59,6 +73,7 @@ struct akua_pbf {
     uint32_t graph_options = 0;
     const char* graph_aos = nullptr;
     size_t graph_stride = 0;
+    int graph_sp_bits = -1;
     int graph_captures = 0;
     int body_launches = 0;
 
@@ -90,15 +105,17 @@ cudaError_t dalloc(akua_pbf* s, T** p, size_t count) {
 }
 
 void free_all(akua_pbf* s) {
-    void* ptrs[] = {s->d_params, s->x4, s->v4, s->col4, s->x4g, s->v4g, s->col4g, s->ps0, s->ps1,
-                    s->dp4, s->dpg, s->vstar4, s->om4, s->vc4, s->size, s->sizeg, s->rho, s->lam,
-                    s->rhog, s->lamg, s->keys0, s->vals0, s->keys1, s->vals1, s->table, s->nbr,
-                    s->cnt, s->counts, s->flags, s->staging};
+    void* ptrs[] = {s->d_params, s->x4, s->v4, s->col4, s->size, s->rref, s->rho, s->lam, s->dp4,
+                    s->x4g, s->col4g, s->ps0, s->ps1, s->vstar4, s->om4, s->vc4, s->dpg, s->xref,
+                    s->sizeg, s->rhog, s->lamg, s->rrefg, s->inv, s->r2i, s->blen, s->order,
+                    s->ka0, s->va0, s->ka1, s->va1, s->kb0, s->vb0, s->kb1, s->vb1,
+                    s->sort_scratch, s->table, s->nbr, s->cnt, s->flags, s->staging};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (s->exec) cudaGraphExecDestroy(s->exec);
     if (s->graph) cudaGraphDestroy(s->graph);
     if (s->capture_stream) cudaStreamDestroy(s->capture_stream);
+    for (cudaEvent_t ev : s->prof_events) cudaEventDestroy(ev);
 }
 
 struct DeviceGuard {
@@ -116,8 +133,21 @@ bool finite3(const float* v) {
     return v && std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]);
 }
 
-// Kernel constants, evaluated once per step on the host in the order the device and the host
-// restatement use.  Host code is compiled with -ffp-contract=off.
+// Bits per axis of the Morton key for a box, and the lowest cell it counts from.
+int morton_bits(const akua_pbf* s, const float* bmin, const float* bmax, int origin[3]) {
+    const double cell = (double)s->cfg.spatialHashCellSize;
+    double extent = 0.0;
+    for (int a = 0; a < 3; ++a) {
+        origin[a] = (int)std::floor((double)bmin[a] / cell) - 1;
+        extent = std::max(extent, ((double)bmax[a] - (double)bmin[a]) / cell + 3.0);
+    }
+    int bits = 1;
+    while (bits < 10 && (double)(1 << bits) < extent) ++bits;
+    return bits;
+}
+
+// Kernel constants, evaluated on the host in the order the device and the host restatement use.
+// Host code is compiled with -ffp-contract=off.
 StepParams make_params(const akua_pbf* s, float dt, const float* bmin, const float* bmax) {
     StepParams p{};
     const float h = s->cfg.smoothRadius;
@@ -158,6 +188,8 @@ StepParams make_params(const akua_pbf* s, float dt, const float* bmin, const flo
     p.n = s->n;
     p.cap = s->cfg.maxNeighbours;
     p.table_size = s->table_size;
+    p.table_magic = UINT64_MAX / (uint64_t)s->table_size + 1u;
+    p.sp_bits = morton_bits(s, bmin, bmax, p.sp_origin);
     return p;
 }
 
@@ -185,9 +217,9 @@ void enqueue_pairs(akua_pbf* s, cudaStream_t st, Marker& mark) {
     const int gp = grid_for(n, akua::kPairBlock);
     const int iters = s->cfg.solverIterations;
     float4* ps[2] = {s->ps0, s->ps1};
-    akua::k_search<EXACT><<<gp, akua::kPairBlock, 0, st>>>(s->d_params, s->ps0, s->sorted_keys,
-                                                           s->table, s->nbr, s->cnt, s->rho, s->lam,
-                                                           s->flags, iters > 0 ? 1 : 0);
+    akua::k_search<EXACT><<<gp, akua::kPairBlock, 0, st>>>(
+        s->d_params, s->ps0, s->xref, s->kr, s->table, s->blen, s->r2i, s->rrefg, s->nbr, s->cnt,
+        s->rho, s->lam, s->flags, iters > 0 ? 1 : 0);
     mark("k_search");
     for (int it = 0; it < iters; ++it) {
         float4* cur = ps[it & 1];
@@ -204,14 +236,16 @@ void enqueue_pairs(akua_pbf* s, cudaStream_t st, Marker& mark) {
         } else {
             akua::k_delta_final<EXACT><<<gp, akua::kPairBlock, 0, st>>>(
                 s->d_params, cur, s->lam, s->nbr, s->cnt, s->x4g, s->x4, s->v4, s->vstar4, s->dp4,
-                s->col4g, s->sizeg, s->col4, s->size, 1);
+                s->col4g, s->sizeg, s->col4, s->size, s->rrefg, s->rref, s->rhog, s->lamg, s->dpg,
+                s->rho, s->lam, 1);
             mark("k_delta_final");
         }
     }
     if (iters == 0) {
         akua::k_delta_final<EXACT><<<gp, akua::kPairBlock, 0, st>>>(
             s->d_params, s->ps0, s->lam, s->nbr, s->cnt, s->x4g, s->x4, s->v4, s->vstar4, s->dp4,
-            s->col4g, s->sizeg, s->col4, s->size, 0);
+            s->col4g, s->sizeg, s->col4, s->size, s->rrefg, s->rref, s->rhog, s->lamg, s->dpg,
+            s->rho, s->lam, 0);
         mark("k_delta_final");
     }
     akua::k_vorticity<EXACT><<<gp, akua::kPairBlock, 0, st>>>(s->d_params, s->x4, s->v4, s->nbr,
@@ -230,33 +264,33 @@ void enqueue_body(akua_pbf* s, cudaStream_t st, const char* aos, size_t stride, 
     const int ge = grid_for(n, akua::kElemBlock);
     Marker mark{s, st, record};
     const bool carry = s->cfg.solverIterations == 0;
-    akua::k_predict_hash<<<ge, akua::kElemBlock, 0, st>>>(s->d_params, s->x4, s->v4, s->keys0);
-    mark("k_predict_hash");
-    akua::radix::sort_pairs(st, s->keys0, s->vals0, s->keys1, s->vals1, s->counts, n, s->passes,
-                            mark);
+    akua::k_keys<<<ge, akua::kElemBlock, 0, st>>>(s->d_params, s->x4, s->v4, s->rref, s->ka0,
+                                                  s->va0, s->kb0);
+    mark("k_keys");
+    uint32_t* dummy = nullptr;
+    akua::radix::sort_pairs(st, s->plan_ref, s->ka0, s->va0, s->ka1, s->va1, false,
+                            s->sort_scratch, n, &s->kr, &s->refperm, mark);
+    akua::radix::sort_pairs(st, s->plan_sp, s->kb0, s->vb0, s->kb1, s->vb1, true, s->sort_scratch,
+                            n, &dummy, &s->spperm, mark);
     akua::k_gather<<<ge, akua::kElemBlock, 0, st>>>(
-        s->d_params, s->sorted_perm, s->x4, s->v4, s->col4, s->size, s->x4g, s->v4g, s->col4g,
-        s->sizeg, s->ps0, s->rhog, s->lamg, s->dpg, s->rho, s->lam, s->dp4, carry ? 1 : 0);
+        s->d_params, s->spperm, s->x4, s->v4, s->col4, s->size, s->x4g, s->col4g, s->sizeg,
+        s->ps0, s->inv, s->rho, s->lam, s->dp4, s->rhog, s->lamg, s->dpg, carry ? 1 : 0);
     mark("k_gather");
-    akua::k_build_table<<<ge, akua::kElemBlock, 0, st>>>(s->d_params, s->sorted_keys, s->table);
-    mark("k_build_table");
-    // v4g holds the sorted velocities; k_delta_final writes the damped ones into v4.
+    akua::k_ref<<<ge, akua::kElemBlock, 0, st>>>(s->d_params, s->kr, s->refperm, s->inv, s->ps0,
+                                                 s->rref, s->r2i, s->rrefg, s->xref, s->table,
+                                                 s->order);
+    mark("k_ref");
+    akua::k_bucket_len<<<ge, akua::kElemBlock, 0, st>>>(s->d_params, s->kr, s->table, s->blen);
+    mark("k_bucket_len");
     if (s->options & AKUA_PBF_OPT_EXACT_MATH) enqueue_pairs<true>(s, st, mark);
     else enqueue_pairs<false>(s, st, mark);
     if (aos) {
-        akua::k_export<<<ge, akua::kElemBlock, 0, st>>>(const_cast<char*>(aos), stride, n, s->x4,
-                                                        s->v4, s->vstar4, s->dp4, s->om4, s->rho,
-                                                        s->lam, s->sorted_keys, s->col4, s->size);
+        akua::k_export<<<grid_for(n, akua::kIoBlock), akua::kIoBlock, 0, st>>>(
+            const_cast<char*>(aos), stride, n, s->r2i, s->kr, s->x4, s->v4, s->vstar4, s->dp4,
+            s->om4, s->rho, s->lam, s->col4, s->size);
         mark("k_export");
     }
     s->body_launches = mark.launches;
-}
-
-void update_sort_layout(akua_pbf* s) {
-    s->passes = akua::radix::passes_for(s->table_size);
-    const bool odd = (s->passes & 1) != 0;
-    s->sorted_keys = odd ? s->keys1 : s->keys0;
-    s->sorted_perm = odd ? s->vals1 : s->vals0;
 }
 
 void invalidate_graph(akua_pbf* s) {
@@ -267,9 +301,15 @@ void invalidate_graph(akua_pbf* s) {
     s->graph_ok = false;
 }
 
+void update_plans(akua_pbf* s, int sp_bits) {
+    s->plan_ref = akua::radix::make_plan(akua::radix::bits_for(s->table_size));
+    s->sp_bits = sp_bits;
+    s->plan_sp = akua::radix::make_plan(3 * sp_bits);
+}
+
 int ensure_graph(akua_pbf* s, const char* aos, size_t stride) {
     if (s->graph_ok && s->graph_options == s->options && s->graph_aos == aos &&
-        s->graph_stride == stride)
+        s->graph_stride == stride && s->graph_sp_bits == s->sp_bits)
         return AKUA_OK;
     invalidate_graph(s);
     cudaError_t e = cudaStreamBeginCapture(s->capture_stream, cudaStreamCaptureModeThreadLocal);
@@ -289,6 +329,7 @@ int ensure_graph(akua_pbf* s, const char* aos, size_t stride) {
     s->graph_options = s->options;
     s->graph_aos = aos;
     s->graph_stride = stride;
+    s->graph_sp_bits = s->sp_bits;
     ++s->graph_captures;
     return AKUA_OK;
 }
@@ -299,6 +340,7 @@ int do_step(akua_pbf* s, const char* aos, size_t stride, bool force_import, floa
         return AKUA_ERR_INVALID_ARGUMENT;
     cudaGetLastError();  // clear a stale error of an unrelated call
     const StepParams p = make_params(s, dt, bmin, bmax);
+    if (p.sp_bits != s->sp_bits) update_plans(s, p.sp_bits);
     cudaStream_t st = s->stream;
     const bool prof = s->prof_active && s->prof_steps_left > 0;
     Marker mark{s, st, prof};
@@ -313,8 +355,8 @@ int do_step(akua_pbf* s, const char* aos, size_t stride, bool force_import, floa
     mark("k_set_params");
     const bool import = force_import || !(s->options & AKUA_PBF_OPT_RESIDENT) || !s->state_valid;
     if (import) {
-        akua::k_import<<<grid_for(s->n, akua::kElemBlock), akua::kElemBlock, 0, st>>>(
-            aos, stride, s->n, s->x4, s->v4, s->col4, s->size, s->rho, s->lam, s->dp4,
+        akua::k_import<<<grid_for(s->n, akua::kIoBlock), akua::kIoBlock, 0, st>>>(
+            aos, stride, s->n, s->x4, s->v4, s->col4, s->size, s->rref, s->rho, s->lam, s->dp4,
             s->cfg.solverIterations == 0 ? 1 : 0);
         mark("k_import");
     }
@@ -331,6 +373,7 @@ int do_step(akua_pbf* s, const char* aos, size_t stride, bool force_import, floa
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_status(e);
     s->state_valid = true;
+    s->stepped = true;
     ++s->steps;
     return AKUA_OK;
 }
@@ -383,26 +426,29 @@ int akua_pbf_create(int32_t n, const akua_pbf_config* cfg, const akua_lambda_cor
     cudaGetDevice(&s->device);
     const size_t N = (size_t)n;
     const size_t cap = (size_t)cfg->maxNeighbours;
-    const int tiles = akua::radix::num_tiles(n);
     cudaError_t e = cudaSuccess;
     auto chk = [&](cudaError_t r) {
         if (e == cudaSuccess) e = r;
     };
     chk(dalloc(s, &s->d_params, 1));
     chk(dalloc(s, &s->x4, N)); chk(dalloc(s, &s->v4, N)); chk(dalloc(s, &s->col4, N));
-    chk(dalloc(s, &s->x4g, N)); chk(dalloc(s, &s->v4g, N)); chk(dalloc(s, &s->col4g, N));
+    chk(dalloc(s, &s->size, N)); chk(dalloc(s, &s->rref, N));
+    chk(dalloc(s, &s->rho, N)); chk(dalloc(s, &s->lam, N)); chk(dalloc(s, &s->dp4, N));
+    chk(dalloc(s, &s->x4g, N)); chk(dalloc(s, &s->col4g, N));
     chk(dalloc(s, &s->ps0, N)); chk(dalloc(s, &s->ps1, N));
-    chk(dalloc(s, &s->dp4, N)); chk(dalloc(s, &s->dpg, N));
     chk(dalloc(s, &s->vstar4, N)); chk(dalloc(s, &s->om4, N)); chk(dalloc(s, &s->vc4, N));
-    chk(dalloc(s, &s->size, N)); chk(dalloc(s, &s->sizeg, N));
-    chk(dalloc(s, &s->rho, N)); chk(dalloc(s, &s->lam, N));
-    chk(dalloc(s, &s->rhog, N)); chk(dalloc(s, &s->lamg, N));
-    chk(dalloc(s, &s->keys0, N)); chk(dalloc(s, &s->vals0, N));
-    chk(dalloc(s, &s->keys1, N)); chk(dalloc(s, &s->vals1, N));
+    chk(dalloc(s, &s->dpg, N)); chk(dalloc(s, &s->xref, N));
+    chk(dalloc(s, &s->sizeg, N)); chk(dalloc(s, &s->rhog, N)); chk(dalloc(s, &s->lamg, N));
+    chk(dalloc(s, &s->rrefg, N)); chk(dalloc(s, &s->inv, N)); chk(dalloc(s, &s->r2i, N));
+    chk(dalloc(s, &s->blen, N)); chk(dalloc(s, &s->order, N));
+    chk(dalloc(s, &s->ka0, N)); chk(dalloc(s, &s->va0, N));
+    chk(dalloc(s, &s->ka1, N)); chk(dalloc(s, &s->va1, N));
+    chk(dalloc(s, &s->kb0, N)); chk(dalloc(s, &s->vb0, N));
+    chk(dalloc(s, &s->kb1, N)); chk(dalloc(s, &s->vb1, N));
+    chk(dalloc(s, &s->sort_scratch, akua::radix::scratch_words(n)));
     chk(dalloc(s, &s->table, (size_t)s->table_alloc));
     chk(dalloc(s, &s->nbr, N * cap));
     chk(dalloc(s, &s->cnt, N));
-    chk(dalloc(s, &s->counts, (size_t)akua::radix::RADIX * tiles));
     chk(dalloc(s, &s->flags, 1));
     if (e == cudaSuccess) e = cudaMemset(s->table, 0xff, sizeof(uint32_t) * (size_t)s->table_alloc);
     if (e == cudaSuccess) e = cudaMemset(s->flags, 0, sizeof(uint32_t));
@@ -415,7 +461,7 @@ int akua_pbf_create(int32_t n, const akua_pbf_config* cfg, const akua_lambda_cor
         cudaGetLastError();
         return cuda_status(e);
     }
-    update_sort_layout(s);
+    update_plans(s, 1);
     *out = s;
     return AKUA_OK;
 }
@@ -516,7 +562,7 @@ int akua_pbf_set_table_size(akua_pbf* s, int32_t table_size) {
                                     s->stream);
     if (e != cudaSuccess) return cuda_status(e);
     s->table_size = (uint32_t)table_size;
-    update_sort_layout(s);
+    update_plans(s, s->sp_bits);
     invalidate_graph(s);
     return AKUA_OK;
 }
@@ -562,21 +608,24 @@ int akua_pbf_get_stats(akua_pbf* s, akua_pbf_stats* st) {
 
 int akua_pbf_read_debug(akua_pbf* s, int32_t what, void* dst, size_t bytes) {
     if (!s || !dst) return AKUA_ERR_INVALID_ARGUMENT;
+    if (!s->stepped) return AKUA_ERR_INVALID_ARGUMENT;  // nothing computed yet
     DeviceGuard g(s->device);
     const size_t N = (size_t)s->n;
-    const void* src = nullptr;
+    const size_t cap = (size_t)s->cfg.maxNeighbours;
     size_t need = 0;
     switch (what) {
-        case AKUA_DEBUG_HASHES: src = s->sorted_keys; need = N * 4; break;
-        case AKUA_DEBUG_ORDER: src = s->sorted_perm; need = N * 4; break;
-        case AKUA_DEBUG_NEIGHBOUR_COUNTS: src = s->cnt; need = N * 4; break;
-        case AKUA_DEBUG_NEIGHBOURS: src = s->nbr; need = N * (size_t)s->cfg.maxNeighbours * 4; break;
+        case AKUA_DEBUG_HASHES:
+        case AKUA_DEBUG_ORDER:
+        case AKUA_DEBUG_NEIGHBOUR_COUNTS: need = N * 4; break;
+        case AKUA_DEBUG_NEIGHBOURS: need = N * cap * 4; break;
         case AKUA_DEBUG_PARTICLES: need = N * sizeof(akua_particle); break;
         default: return AKUA_ERR_INVALID_ARGUMENT;
     }
     if (bytes != need) return AKUA_ERR_INVALID_ARGUMENT;
     cudaError_t e = cudaStreamSynchronize(s->stream);
     if (e != cudaSuccess) return cuda_status(e);
+    if (what == AKUA_DEBUG_HASHES) return cuda_status(cudaMemcpy(dst, s->kr, need, cudaMemcpyDeviceToHost));
+    if (what == AKUA_DEBUG_ORDER) return cuda_status(cudaMemcpy(dst, s->order, need, cudaMemcpyDeviceToHost));
     if (what == AKUA_DEBUG_PARTICLES) {
         char* tmp = nullptr;
         e = cudaMalloc(reinterpret_cast<void**>(&tmp), need);
@@ -584,24 +633,42 @@ int akua_pbf_read_debug(akua_pbf* s, int32_t what, void* dst, size_t bytes) {
             cudaGetLastError();
             return cuda_status(e);
         }
-        akua::k_export<<<grid_for(s->n, akua::kElemBlock), akua::kElemBlock, 0, s->stream>>>(
-            tmp, sizeof(akua_particle), s->n, s->x4, s->v4, s->vstar4, s->dp4, s->om4, s->rho,
-            s->lam, s->sorted_keys, s->col4, s->size);
+        akua::k_export<<<grid_for(s->n, akua::kIoBlock), akua::kIoBlock, 0, s->stream>>>(
+            tmp, sizeof(akua_particle), s->n, s->r2i, s->kr, s->x4, s->v4, s->vstar4, s->dp4,
+            s->om4, s->rho, s->lam, s->col4, s->size);
         e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaMemcpyAsync(dst, tmp, need, cudaMemcpyDeviceToHost, s->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
         cudaFree(tmp);
         return cuda_status(e);
     }
-    e = cudaMemcpy(dst, src, need, cudaMemcpyDeviceToHost);
-    return cuda_status(e);
+    // Neighbour data: convert internal indices to reference ranks (the reference's indexing).
+    std::vector<uint32_t> r2i(N), rank(N), cnt(N);
+    e = cudaMemcpy(r2i.data(), s->r2i, N * 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(rank.data(), s->rref, N * 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(cnt.data(), s->cnt, N * 4, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_status(e);
+    uint32_t* out = static_cast<uint32_t*>(dst);
+    if (what == AKUA_DEBUG_NEIGHBOUR_COUNTS) {
+        for (size_t r = 0; r < N; ++r) out[r] = cnt[r2i[r]];
+        return AKUA_OK;
+    }
+    std::vector<uint32_t> nbr(N * cap);
+    e = cudaMemcpy(nbr.data(), s->nbr, N * cap * 4, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_status(e);
+    std::memset(out, 0, need);
+    for (size_t r = 0; r < N; ++r) {
+        const uint32_t i = r2i[r];
+        for (uint32_t k = 0; k < cnt[i] && k < cap; ++k) out[r * cap + k] = rank[nbr[k * N + i]];
+    }
+    return AKUA_OK;
 }
 
 int akua_pbf_kernels_per_step(akua_pbf* s) {
     if (!s) return AKUA_ERR_INVALID_ARGUMENT;
+    if (s->body_launches == 0) return AKUA_ERR_INVALID_ARGUMENT;  // no step issued yet
     // parameter upload + import (when it runs) + the body
     const bool import = !(s->options & AKUA_PBF_OPT_RESIDENT);
-    if (s->body_launches == 0) return AKUA_ERR_INVALID_ARGUMENT;  // no step issued yet
     return 1 + (import ? 1 : 0) + s->body_launches;
 }
 
@@ -610,7 +677,8 @@ int akua_pbf_profile_begin(akua_pbf* s, int32_t max_steps) {
     DeviceGuard g(s->device);
     for (cudaEvent_t ev : s->prof_events) cudaEventDestroy(ev);
     s->prof_events.clear();
-    const size_t per_step = 8 + 3 * (size_t)s->passes + 2 * (size_t)s->cfg.solverIterations + 8;
+    const size_t per_step = 16 + 3 * (size_t)(akua::radix::MAX_PASSES * 2) +
+                            2 * (size_t)s->cfg.solverIterations;
     const size_t total = per_step * (size_t)max_steps;
     s->prof_events.resize(total, nullptr);
     s->prof_names.assign(total, nullptr);

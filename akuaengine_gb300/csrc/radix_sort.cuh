@@ -1,14 +1,15 @@
 // Stable LSD radix sort of (u32 key, u32 value) pairs.
 //
 // Replaces the comparison sort of whole 108-byte particle records in the reference
-// (thrust::sort with a.hash < b.hash, NeighbourSearchCUDA.cu:167-170).  Only the keys and a u32
-// payload move; the particle state is gathered once afterwards.  Stability makes ties keep the
-// incoming order, i.e. the previous step's sorted order, which is what the reference's merge sort
-// yields for equal hashes.
+// (thrust::sort with a.hash < b.hash, NeighbourSearchCUDA.cu:167-170).  Only keys and a u32
+// payload move; particle state is gathered once afterwards.  Stability makes equal keys keep their
+// incoming order — for the cell-hash sort that is the previous step's sorted order, which is what
+// the reference's merge sort yields for equal hashes.
 //
-// Each pass handles RADIX_BITS bits with three kernels: per-tile digit counts, one exclusive scan
-// over the (digit, tile) matrix, and a stable scatter in which warps rank their keys with
-// match.any and per-warp running digit counters in shared memory.
+// A sort of `bits`-bit keys runs ceil(bits / 10) passes of equal digit width (8..10 bits).  Each
+// pass: per-tile digit counts (also accumulated into per-digit totals), one block per digit that
+// turns its row of the (digit, tile) count matrix into global offsets, and a stable scatter in
+// which warps rank their keys with match.any and per-warp running digit counters.
 #pragma once
 
 #include <cstdint>
@@ -17,20 +18,55 @@
 namespace akua {
 namespace radix {
 
-constexpr int RADIX_BITS = 8;
-constexpr int RADIX = 1 << RADIX_BITS;
+constexpr int MAX_BITS = 10;
+constexpr int MAX_RADIX = 1 << MAX_BITS;
 constexpr int BLOCK = 256;
 constexpr int WARPS = BLOCK / 32;
-constexpr int ROUNDS = 16;                 // keys per lane
-constexpr int WARP_ITEMS = ROUNDS * 32;    // 512
-constexpr int TILE = WARPS * WARP_ITEMS;   // 4096 keys per tile
-constexpr int SCAN_BLOCK = 1024;
+constexpr int ROUNDS = 16;                // keys per lane
+constexpr int WARP_ITEMS = ROUNDS * 32;   // 512
+constexpr int TILE = WARPS * WARP_ITEMS;  // 4096 keys per tile
+constexpr int SCAN_BLOCK = 256;
+constexpr int MAX_PASSES = 4;
 
 inline int num_tiles(int n) { return (n + TILE - 1) / TILE; }
 
-// counts[digit * tiles + tile] = number of keys of `tile` whose digit at `shift` is `digit`.
+// Digit width per pass for keys of `bits` significant bits.
+struct Plan {
+    int passes = 0;
+    int width[MAX_PASSES] = {0, 0, 0, 0};
+    int shift[MAX_PASSES] = {0, 0, 0, 0};
+};
+
+inline Plan make_plan(int bits) {
+    Plan p;
+    if (bits < 1) bits = 1;
+    p.passes = (bits + MAX_BITS - 1) / MAX_BITS;
+    int shift = 0, left = bits;
+    for (int k = 0; k < p.passes; ++k) {
+        const int w0 = (left + (p.passes - k) - 1) / (p.passes - k);
+        const int w = w0 < 8 ? (left < 8 ? left : 8) : w0;  // widths below 8 gain nothing
+        p.width[k] = w;
+        p.shift[k] = shift;
+        shift += w;
+        left -= w;
+        if (left <= 0) { p.passes = k + 1; break; }
+    }
+    return p;
+}
+
+inline int bits_for(uint64_t bound) {  // keys are < bound
+    int bits = 0;
+    uint64_t b = bound > 0 ? bound - 1 : 0;
+    while (b) { ++bits; b >>= 1; }
+    return bits < 1 ? 1 : bits;
+}
+
+// counts[d * tiles + tile] = keys of `tile` with digit d; totals[d] += the same.
+template <int BITS>
 __global__ void __launch_bounds__(BLOCK) upsweep(const uint32_t* __restrict__ keys, int n, int shift,
-                                                 uint32_t* __restrict__ counts, int tiles) {
+                                                 uint32_t* __restrict__ counts,
+                                                 uint32_t* __restrict__ totals, int tiles) {
+    constexpr int RADIX = 1 << BITS;
     __shared__ uint32_t hist[WARPS][RADIX];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int t = threadIdx.x; t < WARPS * RADIX; t += BLOCK) (&hist[0][0])[t] = 0;
@@ -39,10 +75,7 @@ __global__ void __launch_bounds__(BLOCK) upsweep(const uint32_t* __restrict__ ke
 #pragma unroll 4
     for (int r = 0; r < ROUNDS; ++r) {
         const int idx = base + r * 32;
-        if (idx < n) {
-            const uint32_t d = (keys[idx] >> shift) & (RADIX - 1);
-            atomicAdd(&hist[warp][d], 1u);
-        }
+        if (idx < n) atomicAdd(&hist[warp][(keys[idx] >> shift) & (RADIX - 1)], 1u);
     }
     __syncthreads();
     for (int d = threadIdx.x; d < RADIX; d += BLOCK) {
@@ -50,67 +83,64 @@ __global__ void __launch_bounds__(BLOCK) upsweep(const uint32_t* __restrict__ ke
 #pragma unroll
         for (int w = 0; w < WARPS; ++w) s += hist[w][d];
         counts[(size_t)d * tiles + blockIdx.x] = s;
+        if (s) atomicAdd(&totals[d], s);
     }
 }
 
-// In-place exclusive scan of `len` counts by one block.
-__global__ void __launch_bounds__(SCAN_BLOCK) scan(uint32_t* __restrict__ counts, int len) {
-    __shared__ uint32_t warp_sums[SCAN_BLOCK / 32];
+// Block d: offsets[d][t] = sum of totals[0..d) + sum of counts[d][0..t).
+__global__ void __launch_bounds__(SCAN_BLOCK) scan_rows(uint32_t* __restrict__ counts,
+                                                        const uint32_t* __restrict__ totals,
+                                                        int tiles) {
+    __shared__ uint32_t red[SCAN_BLOCK / 32];
     __shared__ uint32_t carry_s;
+    const int d = blockIdx.x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (threadIdx.x == 0) carry_s = 0;
-    __syncthreads();
-    constexpr int PER = 4;
-    for (int chunk = 0; chunk < len; chunk += SCAN_BLOCK * PER) {
-        const int i0 = chunk + threadIdx.x * PER;
-        uint32_t v[PER];
-        uint32_t local = 0;
+    uint32_t part = 0;
+    for (int k = threadIdx.x; k < d; k += SCAN_BLOCK) part += totals[k];
 #pragma unroll
-        for (int k = 0; k < PER; ++k) {
-            v[k] = (i0 + k < len) ? counts[i0 + k] : 0u;
-            local += v[k];
-        }
-        // inclusive warp scan of per-thread sums
-        uint32_t incl = local;
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if (lane == 0) red[warp] = part;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t b = 0;
+        for (int w = 0; w < SCAN_BLOCK / 32; ++w) b += red[w];
+        carry_s = b;
+    }
+    __syncthreads();
+    uint32_t* row = counts + (size_t)d * tiles;
+    for (int chunk = 0; chunk < tiles; chunk += SCAN_BLOCK) {
+        const int t = chunk + threadIdx.x;
+        const uint32_t v = t < tiles ? row[t] : 0u;
+        uint32_t incl = v;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
             if (lane >= o) incl += y;
         }
-        if (lane == 31) warp_sums[warp] = incl;
+        __syncthreads();  // red[] reuse
+        if (lane == 31) red[warp] = incl;
         __syncthreads();
-        if (warp == 0) {
-            uint32_t ws = warp_sums[lane];
-            uint32_t wincl = ws;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t y = __shfl_up_sync(0xffffffffu, wincl, o);
-                if (lane >= o) wincl += y;
-            }
-            warp_sums[lane] = wincl - ws;  // exclusive
-        }
-        __syncthreads();
+        uint32_t wpre = 0;
+        for (int w = 0; w < warp; ++w) wpre += red[w];
         const uint32_t carry = carry_s;
-        uint32_t run = carry + warp_sums[warp] + (incl - local);
-#pragma unroll
-        for (int k = 0; k < PER; ++k) {
-            if (i0 + k < len) counts[i0 + k] = run;
-            run += v[k];
-        }
+        if (t < tiles) row[t] = carry + wpre + incl - v;
         __syncthreads();
-        if (threadIdx.x == SCAN_BLOCK - 1) carry_s = run;
+        if (threadIdx.x == SCAN_BLOCK - 1) carry_s = carry + wpre + incl;
         __syncthreads();
     }
 }
 
 // Stable scatter of one tile.  `vals_in == nullptr` means the payload is the key's index.
+template <int BITS>
 __global__ void __launch_bounds__(BLOCK)
     downsweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
               uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, int n, int shift,
               const uint32_t* __restrict__ offsets, int tiles) {
-    __shared__ uint32_t wbase[WARPS][RADIX];
+    constexpr int RADIX = 1 << BITS;
+    extern __shared__ uint32_t wbase_flat[];  // [WARPS][RADIX]
+    uint32_t(*wbase)[RADIX] = reinterpret_cast<uint32_t(*)[RADIX]>(wbase_flat);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int t = threadIdx.x; t < WARPS * RADIX; t += BLOCK) (&wbase[0][0])[t] = 0;
+    for (int t = threadIdx.x; t < WARPS * RADIX; t += BLOCK) wbase_flat[t] = 0;
     __syncthreads();
     const uint32_t lt_mask = (1u << lane) - 1u;
     const int base = blockIdx.x * TILE + warp * WARP_ITEMS + lane;
@@ -120,8 +150,13 @@ __global__ void __launch_bounds__(BLOCK)
     for (int r = 0; r < ROUNDS; ++r) {
         const int idx = base + r * 32;
         const bool valid = idx < n;
-        key[r] = valid ? keys_in[idx] : 0xffffffffu;
+        key[r] = valid ? keys_in[idx] : 0u;
         val[r] = valid ? (vals_in ? vals_in[idx] : (uint32_t)idx) : 0u;
+    }
+#pragma unroll
+    for (int r = 0; r < ROUNDS; ++r) {
+        const int idx = base + r * 32;
+        const bool valid = idx < n;
         const uint32_t d = valid ? ((key[r] >> shift) & (RADIX - 1)) : 0xffffffffu;
         const uint32_t peers = __match_any_sync(0xffffffffu, d);
         uint32_t before = 0;
@@ -132,7 +167,6 @@ __global__ void __launch_bounds__(BLOCK)
         rank[r] = (uint16_t)(before + __popc(peers & lt_mask));
     }
     __syncthreads();
-    // exclusive prefix over warps per digit, plus the tile's global offset
     for (int d = threadIdx.x; d < RADIX; d += BLOCK) {
         uint32_t run = offsets[(size_t)d * tiles + blockIdx.x];
 #pragma unroll
@@ -155,40 +189,58 @@ __global__ void __launch_bounds__(BLOCK)
     }
 }
 
-// Number of passes for keys below `bound` (bound >= 1).
-inline int passes_for(uint32_t bound) {
-    int bits = 0;
-    uint64_t b = (uint64_t)bound - 1;
-    while (b) { ++bits; b >>= 1; }
-    if (bits == 0) bits = 1;
-    return (bits + RADIX_BITS - 1) / RADIX_BITS;
+template <int BITS, class Mark>
+inline void run_pass(cudaStream_t s, const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
+                     uint32_t* vout, uint32_t* counts, uint32_t* totals, int n, int shift,
+                     Mark& mark) {
+    const int tiles = num_tiles(n);
+    constexpr int RADIX = 1 << BITS;
+    upsweep<BITS><<<tiles, BLOCK, 0, s>>>(kin, n, shift, counts, totals, tiles);
+    mark("radix_upsweep");
+    scan_rows<<<RADIX, SCAN_BLOCK, 0, s>>>(counts, totals, tiles);
+    mark("radix_scan");
+    downsweep<BITS><<<tiles, BLOCK, WARPS * RADIX * sizeof(uint32_t), s>>>(kin, vin, kout, vout, n,
+                                                                           shift, counts, tiles);
+    mark("radix_downsweep");
 }
 
-// Sorts keys[0..n) with payload (index on input).  Ping-pongs between (k0, v0) and (k1, v1);
-// returns true if the result ended in (k1, v1).  `counts` holds RADIX * num_tiles(n) words.
-// `mark(name)` is called after every launch.
+// Scratch words the sort needs for n keys: the count matrix plus per-pass digit totals.
+inline size_t scratch_words(int n) {
+    return (size_t)MAX_RADIX * num_tiles(n) + (size_t)MAX_PASSES * MAX_RADIX;
+}
+
+// Sorts (k0, v0) by the low plan bits, ping-ponging with (k1, v1); all four buffers hold n words.
+// With `index_payload` the input payload is each key's index and v0 is not read.  The result
+// buffers are returned through keys_out / vals_out.  `mark(name)` is called after every kernel.
 template <class Mark>
-inline bool sort_pairs(cudaStream_t s, uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1,
-                       uint32_t* counts, int n, int passes, Mark&& mark) {
-    const int tiles = num_tiles(n);
-    uint32_t *kin = k0, *vin = nullptr, *kout = k1, *vout = v1;
-    for (int p = 0; p < passes; ++p) {
-        const int shift = p * RADIX_BITS;
-        upsweep<<<tiles, BLOCK, 0, s>>>(kin, n, shift, counts, tiles);
-        mark("radix_upsweep");
-        scan<<<1, SCAN_BLOCK, 0, s>>>(counts, RADIX * tiles);
-        mark("radix_scan");
-        downsweep<<<tiles, BLOCK, 0, s>>>(kin, vin, kout, vout, n, shift, counts, tiles);
-        mark("radix_downsweep");
-        // next pass reads what this one wrote
-        uint32_t* nk = kout;
-        uint32_t* nv = vout;
-        kout = kin;
-        vout = (vin ? vin : v0);
-        kin = nk;
-        vin = nv;
+inline void sort_pairs(cudaStream_t s, const Plan& plan, uint32_t* k0, uint32_t* v0, uint32_t* k1,
+                       uint32_t* v1, bool index_payload, uint32_t* scratch, int n,
+                       uint32_t** keys_out, uint32_t** vals_out, Mark& mark) {
+    uint32_t* counts = scratch;
+    uint32_t* totals = scratch + (size_t)MAX_RADIX * num_tiles(n);
+    cudaMemsetAsync(totals, 0, sizeof(uint32_t) * MAX_PASSES * MAX_RADIX, s);
+    const uint32_t* kin = k0;
+    const uint32_t* vin = index_payload ? nullptr : v0;
+    uint32_t* kout = k1;
+    uint32_t* vout = v1;
+    for (int p = 0; p < plan.passes; ++p) {
+        uint32_t* tot = totals + (size_t)p * MAX_RADIX;
+        // a digit narrower than 8 bits only occurs in the last pass, where the key's higher
+        // bits are zero, so the 8-bit kernel sorts it correctly
+        if (plan.width[p] <= 8)
+            run_pass<8>(s, kin, vin, kout, vout, counts, tot, n, plan.shift[p], mark);
+        else if (plan.width[p] == 9)
+            run_pass<9>(s, kin, vin, kout, vout, counts, tot, n, plan.shift[p], mark);
+        else
+            run_pass<10>(s, kin, vin, kout, vout, counts, tot, n, plan.shift[p], mark);
+        if (kout == k1) {
+            kin = k1; vin = v1; kout = k0; vout = v0;
+        } else {
+            kin = k0; vin = v0; kout = k1; vout = v1;
+        }
     }
-    return kin == k1;
+    *keys_out = const_cast<uint32_t*>(kin);
+    *vals_out = const_cast<uint32_t*>(vin);
 }
 
 }  // namespace radix
