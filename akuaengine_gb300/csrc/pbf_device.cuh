@@ -26,6 +26,7 @@ struct StepParams {
     float inv_rho0;     // 1.0f / restDensity (ConstraintSolverCUDA.cu:201)
     float relaxation;
     float wdq;          // poly6(delta_q^2)
+    float inv_wdq;      // 1 / wdq (fast math only)
     float neg_k;        // -k
     float corr_n;       // n (float)
     int32_t corr_n_int; // n when it is an integer in [0, 64], else -1

@@ -168,6 +168,7 @@ StepParams make_params(const akua_pbf* s, float dt, const float* bmin, const flo
         const float dq2 = s->corr.delta_q * s->corr.delta_q;
         const float d = p.h2 - dq2;
         p.wdq = dq2 > p.h2 ? 0.0f : p.kp * ((d * d) * d);
+        p.inv_wdq = 1.0f / p.wdq;
     }
     p.neg_k = -s->corr.k;
     p.corr_n = s->corr.n;
@@ -217,6 +218,7 @@ void enqueue_pairs(akua_pbf* s, cudaStream_t st, Marker& mark) {
     const int gp = grid_for(n, akua::kPairBlock);
     const int iters = s->cfg.solverIterations;
     float4* ps[2] = {s->ps0, s->ps1};
+    const uint4* nbr4 = reinterpret_cast<const uint4*>(s->nbr);
     akua::k_search<EXACT><<<gp, akua::kPairBlock, 0, st>>>(
         s->d_params, s->ps0, s->xref, s->kr, s->table, s->blen, s->r2i, s->rrefg, s->nbr, s->cnt,
         s->rho, s->lam, s->flags, iters > 0 ? 1 : 0);
@@ -225,17 +227,17 @@ void enqueue_pairs(akua_pbf* s, cudaStream_t st, Marker& mark) {
         float4* cur = ps[it & 1];
         float4* nxt = ps[(it + 1) & 1];
         if (it > 0) {
-            akua::k_density_lambda<EXACT><<<gp, akua::kPairBlock, 0, st>>>(s->d_params, cur, s->nbr,
+            akua::k_density_lambda<EXACT><<<gp, akua::kPairBlock, 0, st>>>(s->d_params, cur, nbr4,
                                                                            s->cnt, s->rho, s->lam);
             mark("k_density_lambda");
         }
         if (it + 1 < iters) {
             akua::k_delta_correct<EXACT><<<gp, akua::kPairBlock, 0, st>>>(
-                s->d_params, cur, s->lam, s->nbr, s->cnt, nxt, s->dp4);
+                s->d_params, cur, s->lam, nbr4, s->cnt, nxt, s->dp4);
             mark("k_delta_correct");
         } else {
             akua::k_delta_final<EXACT><<<gp, akua::kPairBlock, 0, st>>>(
-                s->d_params, cur, s->lam, s->nbr, s->cnt, s->x4g, s->x4, s->v4, s->vstar4, s->dp4,
+                s->d_params, cur, s->lam, nbr4, s->cnt, s->x4g, s->x4, s->v4, s->vstar4, s->dp4,
                 s->col4g, s->sizeg, s->col4, s->size, s->rrefg, s->rref, s->rhog, s->lamg, s->dpg,
                 s->rho, s->lam, 1);
             mark("k_delta_final");
@@ -243,18 +245,18 @@ void enqueue_pairs(akua_pbf* s, cudaStream_t st, Marker& mark) {
     }
     if (iters == 0) {
         akua::k_delta_final<EXACT><<<gp, akua::kPairBlock, 0, st>>>(
-            s->d_params, s->ps0, s->lam, s->nbr, s->cnt, s->x4g, s->x4, s->v4, s->vstar4, s->dp4,
+            s->d_params, s->ps0, s->lam, nbr4, s->cnt, s->x4g, s->x4, s->v4, s->vstar4, s->dp4,
             s->col4g, s->sizeg, s->col4, s->size, s->rrefg, s->rref, s->rhog, s->lamg, s->dpg,
             s->rho, s->lam, 0);
         mark("k_delta_final");
     }
-    akua::k_vorticity<EXACT><<<gp, akua::kPairBlock, 0, st>>>(s->d_params, s->x4, s->v4, s->nbr,
+    akua::k_vorticity<EXACT><<<gp, akua::kPairBlock, 0, st>>>(s->d_params, s->x4, s->v4, nbr4,
                                                               s->cnt, s->om4);
     mark("k_vorticity");
     akua::k_confine<EXACT><<<gp, akua::kPairBlock, 0, st>>>(s->d_params, s->x4, s->v4, s->om4,
-                                                            s->rho, s->nbr, s->cnt, s->vc4);
+                                                            s->rho, nbr4, s->cnt, s->vc4);
     mark("k_confine");
-    akua::k_xsph<<<gp, akua::kPairBlock, 0, st>>>(s->d_params, s->x4, s->vc4, s->nbr, s->cnt, s->v4);
+    akua::k_xsph<<<gp, akua::kPairBlock, 0, st>>>(s->d_params, s->x4, s->vc4, nbr4, s->cnt, s->v4);
     mark("k_xsph");
 }
 
@@ -447,7 +449,7 @@ int akua_pbf_create(int32_t n, const akua_pbf_config* cfg, const akua_lambda_cor
     chk(dalloc(s, &s->kb1, N)); chk(dalloc(s, &s->vb1, N));
     chk(dalloc(s, &s->sort_scratch, akua::radix::scratch_words(n)));
     chk(dalloc(s, &s->table, (size_t)s->table_alloc));
-    chk(dalloc(s, &s->nbr, N * cap));
+    chk(dalloc(s, &s->nbr, N * 4 * ((cap + 3) / 4)));  // uint4 tiles of 4 entries
     chk(dalloc(s, &s->cnt, N));
     chk(dalloc(s, &s->flags, 1));
     if (e == cudaSuccess) e = cudaMemset(s->table, 0xff, sizeof(uint32_t) * (size_t)s->table_alloc);
@@ -653,13 +655,15 @@ int akua_pbf_read_debug(akua_pbf* s, int32_t what, void* dst, size_t bytes) {
         for (size_t r = 0; r < N; ++r) out[r] = cnt[r2i[r]];
         return AKUA_OK;
     }
-    std::vector<uint32_t> nbr(N * cap);
-    e = cudaMemcpy(nbr.data(), s->nbr, N * cap * 4, cudaMemcpyDeviceToHost);
+    const size_t words = N * 4 * ((cap + 3) / 4);
+    std::vector<uint32_t> nbr(words);
+    e = cudaMemcpy(nbr.data(), s->nbr, words * 4, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_status(e);
     std::memset(out, 0, need);
     for (size_t r = 0; r < N; ++r) {
         const uint32_t i = r2i[r];
-        for (uint32_t k = 0; k < cnt[i] && k < cap; ++k) out[r * cap + k] = rank[nbr[k * N + i]];
+        for (uint32_t k = 0; k < cnt[i] && k < cap; ++k)
+            out[r * cap + k] = rank[nbr[4 * ((size_t)(k >> 2) * N + i) + (k & 3)]];
     }
     return AKUA_OK;
 }

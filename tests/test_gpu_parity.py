@@ -182,7 +182,7 @@ POS_ATOL = 2e-5        # position units (boxes are 6-15 units wide)
 VEL_ATOL = 4e-3        # = POS_ATOL / dt plus XSPH/vorticity terms
 RHO_RTOL = 2e-5
 LAM_ATOL = 2e-8        # lambda magnitudes are ~1e-4
-VORT_ATOL = 5e-3
+VORT_RTOL = 1e-3      # of the largest |omega|: omega sums nearly cancelling terms of ~|dv| |grad W|
 
 
 def assert_close_fast(g, o):
@@ -194,14 +194,15 @@ def assert_close_fast(g, o):
         "new_velocity": np.abs(g["new_velocity"] - o["new_velocity"]).max(),
         "density": (np.abs(g["density"] - o["density"]) / np.abs(o["density"])).max(),
         "lambda": np.abs(g["lambda"] - o["lambda"]).max(),
-        "vorticity": np.abs(g["vorticity"] - o["vorticity"]).max(),
+        "vorticity": np.abs(g["vorticity"] - o["vorticity"]).max()
+        / max(np.abs(o["vorticity"]).max(), 1e-30),
     }
     print("fast-vs-oracle max errors:", {k: float(v) for k, v in err.items()})
     assert err["position"] <= POS_ATOL
     assert err["velocity"] <= VEL_ATOL and err["new_velocity"] <= VEL_ATOL
     assert err["density"] <= RHO_RTOL
     assert err["lambda"] <= LAM_ATOL
-    assert err["vorticity"] <= VORT_ATOL
+    assert err["vorticity"] <= VORT_RTOL
 
 
 def test_fast_one_step_27k():
