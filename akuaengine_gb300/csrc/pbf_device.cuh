@@ -94,27 +94,6 @@ __device__ __forceinline__ float poly6(const StepParams& p, float r2) {
     return r2 > p.h2 ? 0.0f : w;
 }
 
-// Gradient of the spiky kernel (SmoothingKernelsCUDA.h:23-28): zero when |r| > h or |r| < 1e-5,
-// else ks * (h - |r|)^2 * r / |r|.  EXACT: IEEE sqrt and three IEEE divides, as the reference.
-// Fast: one reciprocal square root; the thresholds are tested on r^2.
-template <bool EXACT>
-__device__ __forceinline__ float3 spiky_grad(const StepParams& p, float sx, float sy, float sz) {
-    const float r2 = len2(sx, sy, sz);
-    if constexpr (EXACT) {
-        const float r = __fsqrt_rn(r2);
-        if (r > p.h || r < 1e-5f) return make_float3(0.f, 0.f, 0.f);
-        const float q = p.h - r;
-        const float c = p.ks * (q * q);
-        return make_float3(__fdiv_rn(c * sx, r), __fdiv_rn(c * sy, r), __fdiv_rn(c * sz, r));
-    } else {
-        const float ir = rsqrtf(r2);
-        const float r = r2 * ir;
-        const float q = p.h - r;
-        const float c = (r2 > p.h2 || r2 < 1e-10f) ? 0.0f : p.ks * (q * q) * ir;
-        return make_float3(c * sx, c * sy, c * sz);
-    }
-}
-
 // Integer power by binary exponentiation (same multiplication pattern as the host restatement).
 __device__ __forceinline__ float pown(float x, int n) {
     float result = 1.0f;
@@ -129,23 +108,6 @@ __device__ __forceinline__ float pown(float x, int n) {
         if (n) base = base * base;
     }
     return result;
-}
-
-// Artificial pressure s_corr = -k * (W(r2) / W(dq^2))^n (ConstraintSolverCUDA.cu:123-124).
-template <bool EXACT>
-__device__ __forceinline__ float scorr(const StepParams& p, float r2) {
-    const float w = poly6(p, r2);
-    const float ratio = EXACT ? __fdiv_rn(w, p.wdq) : __fdividef(w, p.wdq);
-    float pw;
-    if (p.corr_n_int == 4) {
-        const float r_2 = ratio * ratio;
-        pw = r_2 * r_2;
-    } else if (p.corr_n_int >= 0) {
-        pw = pown(ratio, p.corr_n_int);
-    } else {
-        pw = powf(ratio, p.corr_n);
-    }
-    return p.neg_k * pw;
 }
 
 }  // namespace akua

@@ -138,9 +138,9 @@ __global__ void __launch_bounds__(128)
     lam_out[i] = acc.lambda(p);
 }
 
-// s_corr of two pairs (ConstraintSolverCUDA.cu:123-124).
+// (W(r2) / W(dq^2))^n of two pairs: the power in s_corr = -k * (...)^n (ConstraintSolverCUDA.cu:124).
 template <bool EXACT>
-__device__ __forceinline__ float2 scorr2(const StepParams& p, float2 r2) {
+__device__ __forceinline__ float2 scorr_pow2(const StepParams& p, float2 r2) {
     const float2 w = poly6_2(p, r2);
     float2 ratio;
     if (EXACT) ratio = make_float2(__fdiv_rn(w.x, p.wdq), __fdiv_rn(w.y, p.wdq));
@@ -154,7 +154,7 @@ __device__ __forceinline__ float2 scorr2(const StepParams& p, float2 r2) {
     } else {
         pw = make_float2(powf(ratio.x, p.corr_n), powf(ratio.y, p.corr_n));
     }
-    return mul2(f2(p.neg_k), pw);
+    return pw;
 }
 
 // Position delta with artificial pressure (ConstraintSolverCUDA.cu:99-130).
@@ -171,8 +171,11 @@ __device__ __forceinline__ float3 position_delta(const StepParams& p, int n, flo
         const float2 sy = sub2(f2(xi.y), make_float2(a.y, b.y));
         const float2 sz = sub2(f2(xi.z), make_float2(a.z, b.z));
         const float2 r2 = len2_2(sx, sy, sz);
-        const float2 sc = scorr2<EXACT>(p, r2);
-        const float2 bb = mul2(add2(add2(f2(li), lj), sc), make_float2(a.w, b.w));
+        // (lambda_i + lambda_j + s_corr) * m_j with s_corr = -k * pw: the product feeds the sum
+        // and is contracted into it, as the CUDA compiler does with the reference's expression
+        // (ConstraintSolverCUDA.cu:124-126).
+        const float2 pw = scorr_pow2<EXACT>(p, r2);
+        const float2 bb = mul2(fma2(f2(p.neg_k), pw, add2(f2(li), lj)), make_float2(a.w, b.w));
         float2 gx, gy, gz;
         spiky2<EXACT>(p, sx, sy, sz, r2, gx, gy, gz);
         dx = __fmaf_rn(bb.x, gx.x, dx);

@@ -351,8 +351,9 @@ int step_impl(const OracleParams& P, int n, ParticleRec* particles, uint32_t* ou
                 const V3<R> sep = sub(xs[i], xs[j]);
                 const R ratio = K.poly6(dot3<FMA>(sep, sep)) / wdq;
                 const R pw = n_int ? pown(ratio, n_i) : (R)std::pow(ratio, (R)P.corr_n);
-                const R scorr = neg_k * pw;
-                const R b = ((lam[i] + lam[j]) + scorr) * m[j];
+                // lambda_corr = -k * pw is a product used once as an addend: contracted into
+                // (lambda_i + lambda_j) + lambda_corr like every a*b + c of the reference
+                const R b = fmac<FMA>(neg_k, pw, lam[i] + lam[j]) * m[j];
                 const V3<R> g = K.spiky(sep);
                 d = {fmac<FMA>(b, g.x, d.x), fmac<FMA>(b, g.y, d.y), fmac<FMA>(b, g.z, d.z)};
             }
