@@ -38,11 +38,19 @@ CASES = {
 }
 
 
+def tagged(sc):
+    """Particles with colour.r = their input index: colour is carried unchanged through the step,
+    so the output colours spell out the sorted order."""
+    p = sc.particles.copy()
+    p["color"][:, 0] = np.arange(sc.n, dtype=np.float32)
+    return p
+
+
 def main(out_dir):
     os.makedirs(out_dir, exist_ok=True)
     for name, (make, cfg, corr, steps, lists) in CASES.items():
         sc = make()
-        p = sc.particles.copy()
+        p = tagged(sc)
         info = ref_gpu.run(p, params(cfg, corr, sc, sc.n), steps, dump_lists=lists)
         out = {"hash": p["hash"], "position": p["position"], "velocity": p["velocity"],
                "new_velocity": p["new_velocity"], "position_delta": p["position_delta"],

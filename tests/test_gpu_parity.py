@@ -322,3 +322,34 @@ def test_errors_are_reported():
             s.step_host(sc.particles.copy(), -1.0, sc.box_min, sc.box_max)
         with pytest.raises(ak.AkuaError):
             s.set_options(0x80)
+
+
+# --- against the reference's own kernels (fixtures from tests/golden/make_ref_gpu_golden.py) ----
+
+def _ref_cases():
+    import os
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    sys.path.insert(0, os.path.join(here, "golden"))
+    from make_ref_gpu_golden import CASES
+    return CASES
+
+
+@pytest.mark.parametrize("opts", [0, ak.OPT_EXACT_MATH], ids=["fast", "exact"])
+@pytest.mark.parametrize("name", list(_ref_cases()))
+def test_cuda_matches_reference_kernels(name, opts):
+    from make_ref_gpu_golden import tagged
+    from test_reference_golden import compare_floats, load
+
+    make, cfg, corr, steps, lists = _ref_cases()[name]
+    ref = load(name)
+    sc = make()
+    g, ge = run_gpu(sc, cfg, corr, steps, opts, particles=tagged(sc))
+    assert np.array_equal(g["hash"], ref["hash"])
+    assert np.array_equal(g["color"], ref["color"]), "sorted order differs"
+    if lists:
+        assert np.array_equal(ge["cnt"], ref["cnt"])
+        flat = np.concatenate([ge["nbr"][i, : ge["cnt"][i]] for i in range(sc.n)])
+        assert np.array_equal(flat, ref["nbr_flat"])
+    # the fast path adds its own rsqrt-level error on top of the oracle's
+    compare_floats(g, ref, scale=1.0 if opts else 3.0)
