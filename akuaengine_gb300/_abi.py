@@ -121,6 +121,7 @@ _SIGS = {
     "akua_pbf_profile_begin": (ctypes.c_int, [_P, ctypes.c_int32]),
     "akua_pbf_profile_end": (ctypes.c_int, [_P, ctypes.POINTER(CKernelTime), ctypes.c_int32,
                                             ctypes.POINTER(ctypes.c_int32)]),
+    "akua_sort_pairs_noalloc": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int32, ctypes.c_int32, _P]),
     "akua_pbf_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "akua_pbf_abi_version": (ctypes.c_int, []),
 }

@@ -30,7 +30,7 @@ def nvcc_path() -> str:
 
 
 def sources() -> list[str]:
-    return [os.path.join(CSRC, "pbf_solver.cu")]
+    return [os.path.join(CSRC, "pbf_solver.cu"), os.path.join(CSRC, "sort_noalloc.cu")]
 
 
 def headers() -> list[str]:

@@ -16,7 +16,7 @@ HEADER = os.path.join(ROOT, "include", "akua_pbf.h")
 def header_functions():
     text = open(HEADER).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(akua_pbf_\w+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(akua_\w+)\s*\(", text)))
 
 
 def test_library_exports_every_header_symbol(cuda_lib):
