@@ -35,6 +35,7 @@
 
 #include "pbf_device.cuh"
 #include "pbf_pairs.cuh"
+#include "pbf_search.cuh"
 
 namespace akua {
 
@@ -120,11 +121,11 @@ __device__ __forceinline__ uint32_t morton_key(const StepParams& p, int cx, int 
 }
 
 // Cell hash of the predicted position, scattered into the previous reference order so the stable
-// sort ties like the reference's; plus the Morton key of the walk cell.
+// sort ties like the reference's; and the Morton key of the walk cell, by current internal index.
 __global__ void __launch_bounds__(kElemBlock)
     k_keys(const StepParams* __restrict__ P, const float4* __restrict__ x4,
            const float4* __restrict__ v4, const uint32_t* __restrict__ rref,
-           uint32_t* __restrict__ akey, uint32_t* __restrict__ aval, uint32_t* __restrict__ skey) {
+           uint32_t* __restrict__ akey, uint32_t* __restrict__ aval, uint32_t* __restrict__ mkey) {
     const StepParams& p = *P;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
@@ -134,32 +135,51 @@ __global__ void __launch_bounds__(kElemBlock)
     const uint32_t r = rref[i];
     akey[r] = h;
     aval[r] = (uint32_t)i;
-    skey[i] = morton_key(p, cell_coord(xs.x, p.search_cell), cell_coord(xs.y, p.search_cell),
+    mkey[i] = morton_key(p, cell_coord(xs.x, p.search_cell), cell_coord(xs.y, p.search_cell),
                          cell_coord(xs.z, p.search_cell));
 }
 
-// Moves the state into the new internal order and writes the predicted positions.
-// inv[old index] = new index.
+// Morton keys laid out in the new reference order.  Sorting them stably keeps the particles of one
+// cell in reference-rank order inside the internal order, so a bucket that holds a single cell is
+// a contiguous run of internal slots.
 __global__ void __launch_bounds__(kElemBlock)
-    k_gather(const StepParams* __restrict__ P, const uint32_t* __restrict__ perm,
-             const float4* __restrict__ x4, const float4* __restrict__ v4,
-             const float4* __restrict__ col4, const float* __restrict__ size,
+    k_morton_ref(const StepParams* __restrict__ P, const uint32_t* __restrict__ refperm,
+                 const uint32_t* __restrict__ mkey, uint32_t* __restrict__ skey) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= P->n) return;
+    skey[r] = mkey[refperm[r]];
+}
+
+// Moves the state into the new internal order (slot s holds the particle of reference rank
+// spr[s]) and writes the predicted positions, both maps between ranks and slots, the
+// reference-ordered predicted positions and the debug order (pre-sort record index per rank).
+__global__ void __launch_bounds__(kElemBlock)
+    k_gather(const StepParams* __restrict__ P, const uint32_t* __restrict__ spr,
+             const uint32_t* __restrict__ refperm, const float4* __restrict__ x4,
+             const float4* __restrict__ v4, const float4* __restrict__ col4,
+             const float* __restrict__ size, const uint32_t* __restrict__ rref_old,
              float4* __restrict__ x4g, float4* __restrict__ col4g, float* __restrict__ sizeg,
-             float4* __restrict__ ps0, uint32_t* __restrict__ inv,
+             float4* __restrict__ ps0, uint32_t* __restrict__ r2i, uint32_t* __restrict__ rank_of,
+             float4* __restrict__ xref, uint32_t* __restrict__ order_out,
              const float* __restrict__ rho_in, const float* __restrict__ lam_in,
              const float4* __restrict__ dp_in, float* __restrict__ rho_out,
              float* __restrict__ lam_out, float4* __restrict__ dp_out, int carry) {
     const StepParams& p = *P;
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= p.n) return;
-    const uint32_t o = perm[s];
+    const uint32_t r = spr[s];
+    const uint32_t o = refperm[r];
     const float4 x = x4[o];
     const float3 xs = predict(p, x, v4[o]);
+    const float4 q = make_float4(xs.x, xs.y, xs.z, x.w);
     x4g[s] = x;
     col4g[s] = col4[o];
     sizeg[s] = size[o];
-    ps0[s] = make_float4(xs.x, xs.y, xs.z, x.w);
-    inv[o] = (uint32_t)s;
+    ps0[s] = q;
+    r2i[r] = (uint32_t)s;
+    rank_of[s] = r;
+    xref[r] = q;
+    order_out[r] = rref_old[o];
     if (carry) {
         rho_out[s] = rho_in[o];
         lam_out[s] = lam_in[o];
@@ -167,135 +187,65 @@ __global__ void __launch_bounds__(kElemBlock)
     }
 }
 
-// Per reference rank r: internal index, reference-ordered predicted positions, the next step's
-// reference rank of each particle, and the bucket starts: table[hash] = first rank carrying it
-// (NeighbourSearchCUDA.cu:52-65).  The table is never cleared; a lookup is valid only if the rank
-// it names still carries the looked-up hash, which holds exactly for this step's hashes.
+// The bucket table (NeighbourSearchCUDA.cu:52-65 builds hash -> first sorted index).  Here an
+// entry is (x, y): y = 0 for a hash no particle carries; otherwise y = bucket length and x = the
+// bucket's first internal slot, or, with bit 31 of y set (a mixed bucket, see k_bucket_meta), its
+// first reference rank.  The table is all-empty between steps: k_table_clear empties this step's
+// entries after the walk.
+
+// Bucket starts: table[hash].x = first rank carrying it (read by k_bucket_meta); clears the
+// bucket's mixed flag.
 __global__ void __launch_bounds__(kElemBlock)
-    k_ref(const StepParams* __restrict__ P, const uint32_t* __restrict__ kr,
-          const uint32_t* __restrict__ refperm, const uint32_t* __restrict__ inv,
-          const float4* __restrict__ ps0, const uint32_t* __restrict__ rref_old,
-          uint32_t* __restrict__ r2i, uint32_t* __restrict__ rref_new, float4* __restrict__ xref,
-          uint32_t* __restrict__ table, uint32_t* __restrict__ order_out) {
+    k_ref_table(const StepParams* __restrict__ P, const uint32_t* __restrict__ kr,
+                uint2* __restrict__ table, uint32_t* __restrict__ bmix) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= P->n) return;
-    const uint32_t o = refperm[r];
-    const uint32_t s = inv[o];
-    r2i[r] = s;
-    rref_new[s] = (uint32_t)r;
-    xref[r] = ps0[s];
-    order_out[r] = rref_old[o];
     const uint32_t k = kr[r];
-    if (r == 0 || kr[r - 1] != k) table[k] = (uint32_t)r;
+    if (r == 0 || kr[r - 1] != k) {
+        table[k] = make_uint2((uint32_t)r, 0u);
+        bmix[r] = 0u;
+    }
 }
 
-// blen[start rank of a bucket] = number of ranks carrying its hash.
+// blen[start] = number of ranks in the bucket; bmix[start] != 0 when the bucket's particles are
+// not one contiguous run of internal slots in rank order (several cells share its hash, or
+// clamped cells share a Morton key).
 __global__ void __launch_bounds__(kElemBlock)
-    k_bucket_len(const StepParams* __restrict__ P, const uint32_t* __restrict__ kr,
-                 const uint32_t* __restrict__ table, uint32_t* __restrict__ blen) {
+    k_bucket_meta(const StepParams* __restrict__ P, const uint32_t* __restrict__ kr,
+                  const uint2* __restrict__ table, const uint32_t* __restrict__ r2i,
+                  uint32_t* __restrict__ blen, uint32_t* __restrict__ bmix) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = P->n;
     if (r >= n) return;
     const uint32_t k = kr[r];
-    if (r == n - 1 || kr[r + 1] != k) {
-        const uint32_t start = table[k];
-        blen[start] = (uint32_t)r + 1u - start;
+    const bool first = r == 0 || kr[r - 1] != k;
+    const uint32_t start = first ? (uint32_t)r : table[k].x;
+    if (!first && r2i[r] != r2i[r - 1] + 1u) atomicOr(&bmix[start], 1u);
+    if (r == n - 1 || kr[r + 1] != k) blen[start] = (uint32_t)r + 1u - start;
+}
+
+// Final table entries for the walk.
+__global__ void __launch_bounds__(kElemBlock)
+    k_table_fill(const StepParams* __restrict__ P, const uint32_t* __restrict__ kr,
+                 const uint32_t* __restrict__ r2i, const uint32_t* __restrict__ blen,
+                 const uint32_t* __restrict__ bmix, uint2* __restrict__ table) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= P->n) return;
+    const uint32_t k = kr[r];
+    if (r == 0 || kr[r - 1] != k) {
+        const uint32_t len = blen[r];
+        table[k] = bmix[r] ? make_uint2((uint32_t)r, len | kMixedBucket) : make_uint2(r2i[r], len);
     }
 }
 
-// Neighbour walk (NeighbourSearchCUDA.cu:72-130) in the reference's order: the 27 cells with dx
-// outer and dz inner, each bucket in reference order, skipping self, accepting
-// |x_i - x_j|^2 < h^2 and stopping at the capacity.  One thread per particle; the nine bucket
-// lookups of one dx are issued together.  The first kSearchStage entries of each list are staged
-// in shared memory and written out as coalesced uint4 tiles.  When `density` is set, the first
-// Jacobi iteration's density and lambda are then accumulated over the staged list (same terms,
-// same order as k_density_lambda).
-constexpr int kSearchBlock = 128;
-constexpr int kSearchStage = 48;            // list entries staged per particle
-constexpr int kSearchRow = kSearchStage + 4;  // row stride in words: 16-byte rows, 13 x 16 B
-
-__device__ __forceinline__ void put_entry(uint32_t* __restrict__ row, uint32_t* __restrict__ nbr,
-                                          int n, int i, int k, uint32_t j) {
-    if (k < kSearchStage) row[k] = j;
-    else nbr[4 * ((size_t)(k >> 2) * n + i) + (k & 3)] = j;
-}
-
-template <bool EXACT>
-__global__ void __launch_bounds__(kSearchBlock)
-    k_search(const StepParams* __restrict__ P, const float4* __restrict__ ps,
-             const float4* __restrict__ xref, const uint32_t* __restrict__ kr,
-             const uint32_t* __restrict__ table, const uint32_t* __restrict__ blen,
-             const uint32_t* __restrict__ r2i, const uint32_t* __restrict__ rank_of,
-             uint32_t* __restrict__ nbr, uint32_t* __restrict__ cnt, float* __restrict__ rho_out,
-             float* __restrict__ lam_out, uint32_t* __restrict__ flags, int density) {
-    __shared__ __align__(16) uint32_t stage[kSearchBlock * kSearchRow];
-    const StepParams& p = *P;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int n = p.n;
-    if (i >= n) return;
-    uint32_t* row = stage + threadIdx.x * kSearchRow;
-    const float4 xi = ps[i];
-    const uint32_t ri = rank_of[i];
-    const int cx = cell_coord(xi.x, p.search_cell);
-    const int cy = cell_coord(xi.y, p.search_cell);
-    const int cz = cell_coord(xi.z, p.search_cell);
-    const int cap = p.cap;
-    int count = 0;
-#pragma unroll
-    for (int dx = -1; dx <= 1; ++dx) {
-        uint32_t st[9], ln[9];
-#pragma unroll
-        for (int e = 0; e < 9; ++e) {
-            ln[e] = cell_hash(cx + dx, cy + e / 3 - 1, cz + e % 3 - 1, p.table_size, p.table_magic);
-            st[e] = __ldg(table + ln[e]);
-        }
-#pragma unroll
-        for (int e = 0; e < 9; ++e) {
-            const uint32_t k = st[e];
-            uint32_t len = 0u, start = 0u;
-            if (k < (uint32_t)n) {
-                if (__ldg(kr + k) == ln[e]) {
-                    len = __ldg(blen + k);
-                    start = k;
-                }
-            }
-            ln[e] = len;
-            st[e] = start;
-        }
-#pragma unroll
-        for (int e = 0; e < 9; ++e) {
-            const uint32_t end = st[e] + ln[e];
-            for (uint32_t r = st[e]; r < end && count < cap; ++r) {
-                const float4 xj = __ldg(xref + r);
-                const float sx = xi.x - xj.x, sy = xi.y - xj.y, sz = xi.z - xj.z;
-                if (r != ri && len2(sx, sy, sz) < p.h2) {
-                    put_entry(row, nbr, n, i, count, __ldg(r2i + r));
-                    ++count;
-                }
-            }
-        }
-    }
-    cnt[i] = (uint32_t)count;
-    if (count >= cap) atomicOr(flags, kFlagCapReached);
-    // staged tiles -> global (a partial last tile carries unused words)
-    const int staged = min(count, kSearchStage);
-    const uint4* row4 = reinterpret_cast<const uint4*>(row);
-    uint4* out4 = reinterpret_cast<uint4*>(nbr);
-    for (int g = 0; g < (staged + 3) >> 2; ++g) out4[(size_t)g * n + i] = row4[g];
-    if (density) {
-        DensityLambda2<EXACT> acc;
-        acc.init(xi.w, p);
-        for (int k = 0; k < count; k += 2) {
-            const uint32_t j0 = k < kSearchStage ? row[k] : nbr[4 * ((size_t)(k >> 2) * n + i) + (k & 3)];
-            const bool two = k + 1 < count;
-            const int k1 = two ? k + 1 : k;
-            const uint32_t j1 = k1 < kSearchStage ? row[k1]
-                                                  : nbr[4 * ((size_t)(k1 >> 2) * n + i) + (k1 & 3)];
-            acc.add2(p, xi, __ldg(ps + j0), __ldg(ps + j1), two);
-        }
-        rho_out[i] = acc.rho;
-        lam_out[i] = acc.lambda(p);
-    }
+// Empties this step's entries, leaving the table all-empty for the next step.
+__global__ void __launch_bounds__(kElemBlock)
+    k_table_clear(const StepParams* __restrict__ P, const uint32_t* __restrict__ kr,
+                  uint2* __restrict__ table) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= P->n) return;
+    const uint32_t k = kr[r];
+    if (r == 0 || kr[r - 1] != k) table[k] = make_uint2(0u, 0u);
 }
 
 // Writes every field of every particle into the attached records in reference order (record r

@@ -54,12 +54,14 @@ struct akua_pbf {
     float4 *x4g = nullptr, *col4g = nullptr, *ps0 = nullptr, *ps1 = nullptr;
     float4 *vstar4 = nullptr, *om4 = nullptr, *vc4 = nullptr, *dpg = nullptr, *xref = nullptr;
     float *sizeg = nullptr, *rhog = nullptr, *lamg = nullptr;
-    uint32_t *rrefg = nullptr, *inv = nullptr, *r2i = nullptr, *blen = nullptr, *order = nullptr;
+    uint32_t *rrefg = nullptr, *mkey = nullptr, *r2i = nullptr, *blen = nullptr, *order = nullptr;
+    uint32_t* bmix = nullptr;  // per bucket start: nonzero when the bucket is not one internal run
     // sorts: reference order (A) and Morton order (B)
     uint32_t *ka0 = nullptr, *va0 = nullptr, *ka1 = nullptr, *va1 = nullptr;
     uint32_t *kb0 = nullptr, *vb0 = nullptr, *kb1 = nullptr, *vb1 = nullptr;
     uint32_t* sort_scratch = nullptr;
-    uint32_t *table = nullptr, *nbr = nullptr, *cnt = nullptr, *flags = nullptr;
+    uint2* table = nullptr;
+    uint32_t *nbr = nullptr, *cnt = nullptr, *flags = nullptr;
     char* staging = nullptr;
     size_t staging_bytes = 0;
 
@@ -107,7 +109,7 @@ cudaError_t dalloc(akua_pbf* s, T** p, size_t count) {
 void free_all(akua_pbf* s) {
     void* ptrs[] = {s->d_params, s->x4, s->v4, s->col4, s->size, s->rref, s->rho, s->lam, s->dp4,
                     s->x4g, s->col4g, s->ps0, s->ps1, s->vstar4, s->om4, s->vc4, s->dpg, s->xref,
-                    s->sizeg, s->rhog, s->lamg, s->rrefg, s->inv, s->r2i, s->blen, s->order,
+                    s->sizeg, s->rhog, s->lamg, s->rrefg, s->mkey, s->r2i, s->blen, s->order, s->bmix,
                     s->ka0, s->va0, s->ka1, s->va1, s->kb0, s->vb0, s->kb1, s->vb1,
                     s->sort_scratch, s->table, s->nbr, s->cnt, s->flags, s->staging};
     for (void* p : ptrs)
@@ -219,10 +221,14 @@ void enqueue_pairs(akua_pbf* s, cudaStream_t st, Marker& mark) {
     const int iters = s->cfg.solverIterations;
     float4* ps[2] = {s->ps0, s->ps1};
     const uint4* nbr4 = reinterpret_cast<const uint4*>(s->nbr);
-    akua::k_search<EXACT><<<gp, akua::kPairBlock, 0, st>>>(
-        s->d_params, s->ps0, s->xref, s->kr, s->table, s->blen, s->r2i, s->rrefg, s->nbr, s->cnt,
-        s->rho, s->lam, s->flags, iters > 0 ? 1 : 0);
+    akua::k_search<EXACT><<<grid_for(n, akua::kSearchBlock), akua::kSearchBlock,
+                            akua::kSearchSmem, st>>>(
+        s->d_params, s->ps0, s->xref, s->table, s->r2i, s->nbr, s->cnt, s->rho, s->lam,
+        s->flags, iters > 0 ? 1 : 0);
     mark("k_search");
+    akua::k_table_clear<<<grid_for(n, akua::kElemBlock), akua::kElemBlock, 0, st>>>(s->d_params,
+                                                                                   s->kr, s->table);
+    mark("k_table_clear");
     for (int it = 0; it < iters; ++it) {
         float4* cur = ps[it & 1];
         float4* nxt = ps[(it + 1) & 1];
@@ -267,23 +273,30 @@ void enqueue_body(akua_pbf* s, cudaStream_t st, const char* aos, size_t stride, 
     Marker mark{s, st, record};
     const bool carry = s->cfg.solverIterations == 0;
     akua::k_keys<<<ge, akua::kElemBlock, 0, st>>>(s->d_params, s->x4, s->v4, s->rref, s->ka0,
-                                                  s->va0, s->kb0);
+                                                  s->va0, s->mkey);
     mark("k_keys");
     uint32_t* dummy = nullptr;
+    // reference order: stable by (hash, previous reference rank)
     akua::radix::sort_pairs(st, s->plan_ref, s->ka0, s->va0, s->ka1, s->va1, false,
                             s->sort_scratch, n, &s->kr, &s->refperm, mark);
+    // internal order: stable by Morton cell over the new reference order; payload = rank
+    akua::k_morton_ref<<<ge, akua::kElemBlock, 0, st>>>(s->d_params, s->refperm, s->mkey, s->kb0);
+    mark("k_morton_ref");
     akua::radix::sort_pairs(st, s->plan_sp, s->kb0, s->vb0, s->kb1, s->vb1, true, s->sort_scratch,
                             n, &dummy, &s->spperm, mark);
     akua::k_gather<<<ge, akua::kElemBlock, 0, st>>>(
-        s->d_params, s->spperm, s->x4, s->v4, s->col4, s->size, s->x4g, s->col4g, s->sizeg,
-        s->ps0, s->inv, s->rho, s->lam, s->dp4, s->rhog, s->lamg, s->dpg, carry ? 1 : 0);
+        s->d_params, s->spperm, s->refperm, s->x4, s->v4, s->col4, s->size, s->rref, s->x4g,
+        s->col4g, s->sizeg, s->ps0, s->r2i, s->rrefg, s->xref, s->order, s->rho, s->lam, s->dp4,
+        s->rhog, s->lamg, s->dpg, carry ? 1 : 0);
     mark("k_gather");
-    akua::k_ref<<<ge, akua::kElemBlock, 0, st>>>(s->d_params, s->kr, s->refperm, s->inv, s->ps0,
-                                                 s->rref, s->r2i, s->rrefg, s->xref, s->table,
-                                                 s->order);
-    mark("k_ref");
-    akua::k_bucket_len<<<ge, akua::kElemBlock, 0, st>>>(s->d_params, s->kr, s->table, s->blen);
-    mark("k_bucket_len");
+    akua::k_ref_table<<<ge, akua::kElemBlock, 0, st>>>(s->d_params, s->kr, s->table, s->bmix);
+    mark("k_ref_table");
+    akua::k_bucket_meta<<<ge, akua::kElemBlock, 0, st>>>(s->d_params, s->kr, s->table, s->r2i,
+                                                         s->blen, s->bmix);
+    mark("k_bucket_meta");
+    akua::k_table_fill<<<ge, akua::kElemBlock, 0, st>>>(s->d_params, s->kr, s->r2i, s->blen,
+                                                        s->bmix, s->table);
+    mark("k_table_fill");
     if (s->options & AKUA_PBF_OPT_EXACT_MATH) enqueue_pairs<true>(s, st, mark);
     else enqueue_pairs<false>(s, st, mark);
     if (aos) {
@@ -441,7 +454,8 @@ int akua_pbf_create(int32_t n, const akua_pbf_config* cfg, const akua_lambda_cor
     chk(dalloc(s, &s->vstar4, N)); chk(dalloc(s, &s->om4, N)); chk(dalloc(s, &s->vc4, N));
     chk(dalloc(s, &s->dpg, N)); chk(dalloc(s, &s->xref, N));
     chk(dalloc(s, &s->sizeg, N)); chk(dalloc(s, &s->rhog, N)); chk(dalloc(s, &s->lamg, N));
-    chk(dalloc(s, &s->rrefg, N)); chk(dalloc(s, &s->inv, N)); chk(dalloc(s, &s->r2i, N));
+    chk(dalloc(s, &s->rrefg, N)); chk(dalloc(s, &s->mkey, N)); chk(dalloc(s, &s->r2i, N));
+    chk(dalloc(s, &s->bmix, N));
     chk(dalloc(s, &s->blen, N)); chk(dalloc(s, &s->order, N));
     chk(dalloc(s, &s->ka0, N)); chk(dalloc(s, &s->va0, N));
     chk(dalloc(s, &s->ka1, N)); chk(dalloc(s, &s->va1, N));
@@ -452,10 +466,17 @@ int akua_pbf_create(int32_t n, const akua_pbf_config* cfg, const akua_lambda_cor
     chk(dalloc(s, &s->nbr, N * 4 * ((cap + 3) / 4)));  // uint4 tiles of 4 entries
     chk(dalloc(s, &s->cnt, N));
     chk(dalloc(s, &s->flags, 1));
-    if (e == cudaSuccess) e = cudaMemset(s->table, 0xff, sizeof(uint32_t) * (size_t)s->table_alloc);
+    if (e == cudaSuccess) e = cudaMemset(s->table, 0, sizeof(uint2) * (size_t)s->table_alloc);
     if (e == cudaSuccess) e = cudaMemset(s->flags, 0, sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemset(s->dp4, 0, sizeof(float4) * N);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->capture_stream, cudaStreamNonBlocking);
+    // the staged neighbour walk needs more than the default 48 KB of dynamic shared memory
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(akua::k_search<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)akua::kSearchSmem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(akua::k_search<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)akua::kSearchSmem);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
         free_all(s);
@@ -547,21 +568,20 @@ int akua_pbf_set_table_size(akua_pbf* s, int32_t table_size) {
     if ((uint32_t)table_size > s->table_alloc) {
         cudaError_t e = cudaStreamSynchronize(s->stream);
         if (e != cudaSuccess) return cuda_status(e);
-        uint32_t* t = nullptr;
-        e = cudaMalloc(reinterpret_cast<void**>(&t), sizeof(uint32_t) * (size_t)table_size);
+        uint2* t = nullptr;
+        e = cudaMalloc(reinterpret_cast<void**>(&t), sizeof(uint2) * (size_t)table_size);
         if (e != cudaSuccess) {
             cudaGetLastError();
             return cuda_status(e);
         }
         cudaFree(s->table);
-        s->device_bytes -= sizeof(uint32_t) * (size_t)s->table_alloc;
-        s->device_bytes += sizeof(uint32_t) * (size_t)table_size;
+        s->device_bytes -= sizeof(uint2) * (size_t)s->table_alloc;
+        s->device_bytes += sizeof(uint2) * (size_t)table_size;
         s->table = t;
         s->table_alloc = (uint32_t)table_size;
     }
-    // A smaller table reuses the allocation; stale entries are rejected by the key check.
-    cudaError_t e = cudaMemsetAsync(s->table, 0xff, sizeof(uint32_t) * (size_t)s->table_alloc,
-                                    s->stream);
+    // A smaller table reuses the allocation, emptied.
+    cudaError_t e = cudaMemsetAsync(s->table, 0, sizeof(uint2) * (size_t)s->table_alloc, s->stream);
     if (e != cudaSuccess) return cuda_status(e);
     s->table_size = (uint32_t)table_size;
     update_plans(s, s->sp_bits);
