@@ -34,31 +34,45 @@ METRIC = "1M-particle PBF steps/s"
 UNIT = "steps/s"
 WORKLOAD = "dam_break_1m"
 
-# Algorithmic bytes per particle moved by each kernel (compulsory traffic of the SoA design;
-# neighbour positions re-read from cache are not counted, neighbour lists are).  `C` stands for
-# the mean neighbour count, filled in from the run.
+# Algorithmic bytes per particle moved by each kernel: the compulsory traffic of the SoA design,
+# every array a kernel reads or writes counted once per particle; neighbour positions gathered
+# through the lists are assumed cache-served and not counted, the lists themselves are.  `L` is
+# the mean bytes of one particle's list tiles (16 * ceil(count / 4)), `B` the mean number of bucket
+# table entries per particle (one 8-byte entry per occupied bucket), both taken from the run.
 KERNEL_BYTES = {
-    "k_import": lambda c: 48 + 52,          # R x,v,m,colour,size of the record; W SoA
-    "k_predict_hash": lambda c: 24 + 4,     # R x, v; W key
-    "radix_upsweep": lambda c: 4,           # R key
-    "radix_downsweep": lambda c: 16,        # R key, value; W key, value
-    "k_gather": lambda c: 4 + 48 + 48 + 12,  # R perm, state; W state, predicted x
-    "k_build_table": lambda c: 4,           # R key
-    "k_search": lambda c: 12 + 4 + 4 * c + 4 + 8,   # R x*, key; W list, count, rho, lambda
-    "k_density_lambda": lambda c: 12 + 4 + 4 + 4 * c + 8,  # R x*, m, count, list; W rho, lambda
-    "k_delta_correct": lambda c: 12 + 4 + 4 + 4 * c + 12 + 12,  # R x*, lambda, count, list; W x*, dp
-    "k_delta_final": lambda c: 12 + 4 + 4 + 4 * c + 12 + 12 + 12 + 12 + 12,  # + R x; W x, v, v*, dp
-    "k_vorticity": lambda c: 12 + 12 + 4 + 4 * c + 12,   # R x, v, count, list; W omega
-    "k_confine": lambda c: 12 + 12 + 12 + 4 + 4 + 4 * c + 16,  # R x, v, omega, rho, count, list; W v
-    "k_xsph": lambda c: 12 + 16 + 4 + 4 * c + 12,        # R x, v+m/rho, count, list; W v
-    "k_export": lambda c: 108,              # W the record
+    # R record 108; W x|m, v, colour, size, rank
+    "k_import": lambda L, B: 108 + 16 + 16 + 16 + 4 + 4,
+    # R x|m, v, rank; W hash key, index, Morton key
+    "k_keys": lambda L, B: 16 + 16 + 4 + 12,
+    "radix_upsweep": lambda L, B: 4,                  # R key (per pass)
+    "radix_downsweep": lambda L, B: 16,               # R key, value; W key, value (per pass)
+    "k_morton_ref": lambda L, B: 12,                  # R permutation, Morton key; W key
+    # R two permutations, x|m, v, colour, size, old rank; W x|m, colour, size, x*|m, rank->slot,
+    # slot->rank, reference-ordered x*|m, order
+    "k_gather": lambda L, B: 8 + 16 + 16 + 16 + 4 + 4 + 16 + 16 + 4 + 16 + 4 + 4 + 16 + 4,
+    "k_ref_table": lambda L, B: 4 + 12 * B,           # R keys; W bucket starts, flags
+    "k_bucket_meta": lambda L, B: 4 + 4 + 12 * B,     # R keys, slots; W lengths, flags
+    "k_table_fill": lambda L, B: 4 + 24 * B,          # R keys; R slot, length, flag; W entry
+    # R x*|m, 27 bucket entries per cell run; W lists, count, rho, lambda
+    "k_search": lambda L, B: 16 + 27 * 8 * B + L + 4 + 8,
+    "k_table_clear": lambda L, B: 4 + 8 * B,          # R keys; W entry
+    "k_density_lambda": lambda L, B: 16 + 4 + L + 8,  # R x*|m, count, lists; W rho, lambda
+    # R x*|m, lambda, count, lists; W x*|m, delta
+    "k_delta_correct": lambda L, B: 16 + 4 + 4 + L + 16 + 16,
+    # R x*|m, lambda, count, lists, x|m, colour, size, rank; W x, v, v*, delta, colour, size, rank
+    "k_delta_final": lambda L, B: 16 + 4 + 4 + L + 16 + 16 + 4 + 4 + 16 * 4 + 16 + 4 + 4,
+    "k_vorticity": lambda L, B: 16 + 16 + 4 + L + 16,        # R x, v, count, lists; W omega
+    "k_confine": lambda L, B: 16 + 16 + 16 + 4 + 4 + L + 16,  # R x, v, omega, rho, count, lists; W v|m/rho
+    "k_xsph": lambda L, B: 16 + 16 + 4 + L + 16,             # R x, v|m/rho, count, lists; W v
+    # R slot, key, x, v, v*, delta, omega, colour, rho, lambda, size; W record 108
+    "k_export": lambda L, B: 4 + 4 + 16 * 6 + 4 + 4 + 4 + 108,
 }
 
 
 def parse_args(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=500)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default=WORKLOAD)
@@ -210,6 +224,7 @@ def run_ours(args, sc, cfg, corr):
     stream = torch.cuda.Stream()
     opts = ak.OPT_EXACT_MATH if args.exact else 0
     solver = PBFSolver(sc.n, cfg, corr, options=opts, stream=stream)
+    table_size = solver.stats()["tableSize"]
     host = sc.particles
     buf = torch.from_numpy(host.view(np.uint8).copy()).cuda()
     torch.cuda.synchronize()
@@ -222,8 +237,11 @@ def run_ours(args, sc, cfg, corr):
         for _ in range(args.warmup):
             solver.step(buf, sc.dt, sc.box_min, sc.box_max)
     torch.cuda.synchronize()
-    cnt = solver.read_debug(ak.DEBUG_NEIGHBOUR_COUNTS)
+    cnt = solver.read_debug(ak.DEBUG_NEIGHBOUR_COUNTS).astype(np.int64)
     mean_c = float(cnt.mean())
+    list_bytes = float((16 * ((cnt + 3) // 4)).mean())
+    hashes = solver.read_debug(ak.DEBUG_HASHES)
+    buckets_per_particle = float(np.unique(hashes).size) / sc.n
 
     # timed region: K steps on the solver's stream, events on that stream
     sampler = ClockSampler(local)
@@ -258,22 +276,29 @@ def run_ours(args, sc, cfg, corr):
                    "share": round(v[1] / total, 4)} for k, v in prof.items()}
     dom = max((k for k in prof if k in KERNEL_BYTES), key=lambda k: prof[k][1])
     per_launch_s = prof[dom][1] / prof[dom][0] / 1000.0
-    alg_bytes = KERNEL_BYTES[dom](mean_c) * sc.n
+    alg = {k: KERNEL_BYTES[k](list_bytes, buckets_per_particle) * sc.n for k in KERNEL_BYTES}
+    alg_bytes = alg[dom]
     peak, peak_kind = load_peaks()
     achieved = alg_bytes / per_launch_s / 1e9
+    for k, v in kernels.items():
+        if k in alg:
+            v["algorithmic_bytes"] = int(alg[k])
+            v["gbs"] = round(alg[k] / (1e-3 * v["ms_total"] / v["launches"]) / 1e9, 1)
+    step_bytes = sum(alg[k] * prof[k][0] for k in prof if k in alg) / args.profile_steps
     traffic = None
     try:
-        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+        with open(os.path.join(ROOT, "profiles", "traffic_%s.json" % args.workload)) as f:
             tr = json.load(f)
-        if dom in tr.get("bytes_per_launch", {}) and tr.get("workload") == args.workload:
-            traffic = tr["bytes_per_launch"][dom]
+        traffic = tr["bytes_per_launch"].get(dom)
     except Exception:
         pass
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
                 "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                "traffic": traffic, "algorithmic_bytes": alg_bytes,
-                "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_kind
-                if peak_kind == "measured" else "fallback 6.8 TB/s"}
+                "traffic": traffic, "algorithmic_bytes": int(alg_bytes),
+                "peak_source": "measured hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured"
+                else "fallback 6.8 TB/s",
+                "step_algorithmic_bytes": int(step_bytes),
+                "step_achieved": round(step_bytes / (ms / args.steps / 1000.0) / 1e9, 1)}
 
     # end to end through the public API: pinned host records -> device, step, -> host
     e2e = None
@@ -311,12 +336,14 @@ def run_ours(args, sc, cfg, corr):
             "data": "synthetic (seeded lattice block + uniform jitter 0.01h)",
             "config": {"workload": args.workload, "particles": sc.n, "block": [100, 100, 100],
                        "box_block_widths": [3.0, 1.5, 1.5], "dt": sc.dt, "solver_iterations": 4,
-                       "max_neighbours": cfg.maxNeighbours, "table_size": cfg.maxNeighbours * sc.n,
+                       "max_neighbours": cfg.maxNeighbours, "table_size": table_size,
                        "corr": {"k": corr.k, "n": corr.n, "delta_q": corr.delta_q},
                        "math": "exact" if args.exact else "fast",
                        "parallelism": "replicas x%d" % world,
                        "l2": "per-step working set > L2 (no flush)",
-                       "mean_neighbours": round(mean_c, 3)},
+                       "mean_neighbours": round(mean_c, 3),
+                       "list_bytes_per_particle": round(list_bytes, 2),
+                       "buckets_per_particle": round(buckets_per_particle, 4)},
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": e2e,
