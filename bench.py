@@ -84,10 +84,10 @@ def parse_args(argv=None):
 
 
 def dist_env():
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", str(rank)))
-    return world, rank, local
+    from akuaengine_gb300 import replicas
+
+    e = replicas.dist_env()
+    return e.world, e.rank, e.local_rank
 
 
 def load_peaks():
@@ -211,7 +211,7 @@ def run_ours(args, sc, cfg, corr):
     import torch
 
     import akuaengine_gb300 as ak
-    from akuaengine_gb300 import PBFSolver
+    from akuaengine_gb300 import PBFSolver, replicas
 
     world, rank, local = dist_env()
     torch.cuda.set_device(local)
@@ -258,11 +258,8 @@ def run_ours(args, sc, cfg, corr):
     clocks = sampler.stop()
     barrier()
     ms = ev0.elapsed_time(ev1)
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * args.steps / (ms / 1000.0)
+    ms = replicas.max_over_ranks(ms, device="cuda")
+    value = replicas.aggregate_rate(args.steps, ms / 1000.0, world)
     launches_per_step = solver.kernels_per_step()
 
     # per-kernel durations (CUDA events between consecutive kernels on the same stream)
@@ -313,11 +310,8 @@ def run_ours(args, sc, cfg, corr):
         for _ in range(args.steps):
             solver.step_host(hp, sc.dt, sc.box_min, sc.box_max)
         el = time.perf_counter() - t0
-        if dist is not None:
-            t = torch.tensor([el], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            el = float(t.item())
-        e2e = {"value": world * args.steps / el, "unit": UNIT,
+        el = replicas.max_over_ranks(el, device="cuda")
+        e2e = {"value": replicas.aggregate_rate(args.steps, el, world), "unit": UNIT,
                "h2d_bytes_per_step": int(host.nbytes), "d2h_bytes_per_step": int(host.nbytes),
                "api": "akua_pbf_step_host (pinned host records)"}
 
@@ -360,7 +354,10 @@ def main(argv=None):
     args = parse_args(argv)
     from akuaengine_gb300 import scene
 
-    sc = scene.workload(args.workload, seed=0)
+    from akuaengine_gb300 import replicas
+
+    # every rank steps its own replica (rank 0: seed 0); replicas exchange no data
+    sc = scene.workload(args.workload, seed=replicas.replica_seed(0, replicas.dist_env().rank))
     cfg, corr = scene.benchmark_params()
     if args.impl == "reference":
         run_reference(args, sc, cfg, corr)
