@@ -22,6 +22,11 @@ OPT_EXACT_MATH = 0x1
 OPT_RESIDENT = 0x2
 OPT_NO_GRAPH = 0x4
 
+MLP_INPUTS = 8
+MLP_HIDDEN = 64
+MLP_PARAMS = 8961
+MLP_NORM = 17
+
 DEBUG_HASHES = 1
 DEBUG_ORDER = 2
 DEBUG_NEIGHBOUR_COUNTS = 3
@@ -122,6 +127,22 @@ _SIGS = {
     "akua_pbf_profile_end": (ctypes.c_int, [_P, ctypes.POINTER(CKernelTime), ctypes.c_int32,
                                             ctypes.POINTER(ctypes.c_int32)]),
     "akua_sort_pairs_noalloc": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int32, ctypes.c_int32, _P]),
+    "akua_pbf_set_solver_iterations": (ctypes.c_int, [_P, ctypes.c_int32]),
+    "akua_mlp_create": (ctypes.c_int, [ctypes.POINTER(_P)]),
+    "akua_mlp_destroy": (ctypes.c_int, [_P]),
+    "akua_mlp_set_params": (ctypes.c_int, [_P, _P, ctypes.c_int32]),
+    "akua_mlp_get_params": (ctypes.c_int, [_P, _P, ctypes.c_int32]),
+    "akua_mlp_set_normalization": (ctypes.c_int, [_P, _P, ctypes.c_int32]),
+    "akua_mlp_forward": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32, _P]),
+    "akua_mlp_gradient": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32, _P,
+                                         ctypes.POINTER(ctypes.c_float), _P]),
+    "akua_mlp_adam_step": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32, ctypes.c_float, _P]),
+    "akua_mlp_synchronize": (ctypes.c_int, [_P, _P]),
+    "akua_pbf_set_warm_start": (ctypes.c_int, [_P, _P]),
+    "akua_pbf_capture_training": (ctypes.c_int, [_P, _P, _P]),
+    "akua_pbf_set_lambda_tracking": (ctypes.c_int, [_P, ctypes.c_int32]),
+    "akua_pbf_density_error": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_float),
+                                              ctypes.POINTER(ctypes.c_float)]),
     "akua_pbf_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "akua_pbf_abi_version": (ctypes.c_int, []),
 }

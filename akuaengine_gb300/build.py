@@ -30,7 +30,8 @@ def nvcc_path() -> str:
 
 
 def sources() -> list[str]:
-    return [os.path.join(CSRC, "pbf_solver.cu"), os.path.join(CSRC, "sort_noalloc.cu")]
+    return [os.path.join(CSRC, "pbf_solver.cu"), os.path.join(CSRC, "sort_noalloc.cu"),
+            os.path.join(CSRC, "mlp.cu")]
 
 
 def headers() -> list[str]:

@@ -163,14 +163,23 @@ __global__ void __launch_bounds__(kElemBlock)
              float4* __restrict__ xref, uint32_t* __restrict__ order_out,
              const float* __restrict__ rho_in, const float* __restrict__ lam_in,
              const float4* __restrict__ dp_in, float* __restrict__ rho_out,
-             float* __restrict__ lam_out, float4* __restrict__ dp_out, int carry) {
+             float* __restrict__ lam_out, float4* __restrict__ dp_out, int carry,
+             const float* __restrict__ lacc_src, float* __restrict__ lprev_out,
+             float4* __restrict__ vstar_out) {
     const StepParams& p = *P;
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= p.n) return;
     const uint32_t r = spr[s];
     const uint32_t o = refperm[r];
     const float4 x = x4[o];
-    const float3 xs = predict(p, x, v4[o]);
+    const float4 v = v4[o];
+    const float3 xs = predict(p, x, v);
+    if (vstar_out) {  // learned modes: predicted velocity and last step's accumulated lambda
+        vstar_out[s] = make_float4(__fmaf_rn(p.gravity[0], p.dt, v.x),
+                                   __fmaf_rn(p.gravity[1], p.dt, v.y),
+                                   __fmaf_rn(p.gravity[2], p.dt, v.z), 0.f);
+        lprev_out[s] = lacc_src[o];
+    }
     const float4 q = make_float4(xs.x, xs.y, xs.z, x.w);
     x4g[s] = x;
     col4g[s] = col4[o];
@@ -257,7 +266,8 @@ __global__ void __launch_bounds__(kIoBlock)
              const float4* __restrict__ v4, const float4* __restrict__ vstar4,
              const float4* __restrict__ dp4, const float4* __restrict__ om4,
              const float* __restrict__ rho, const float* __restrict__ lam,
-             const float4* __restrict__ col4, const float* __restrict__ size) {
+             const float4* __restrict__ col4, const float* __restrict__ size,
+             const float* __restrict__ lacc, float* __restrict__ lacc_ref) {
     __shared__ float rec[kIoBlock * kRecWords];
     const int r0 = blockIdx.x * kIoBlock;
     const int cnt = min(kIoBlock, n - r0);
@@ -265,6 +275,7 @@ __global__ void __launch_bounds__(kIoBlock)
     if (t < cnt) {
         const int r = r0 + t;
         const uint32_t s = r2i[r];
+        if (lacc_ref) lacc_ref[r] = lacc[s];
         const float4 x = x4[s], v = v4[s], vs = vstar4[s], d = dp4[s], w = om4[s], c = col4[s];
         float* o = rec + t * kRecWords;
         o[kPos] = x.x; o[kPos + 1] = x.y; o[kPos + 2] = x.z;

@@ -123,7 +123,8 @@ template <bool EXACT>
 __global__ void __launch_bounds__(128)
     k_density_lambda(const StepParams* __restrict__ P, const float4* __restrict__ ps,
                      const uint4* __restrict__ nbr4, const uint32_t* __restrict__ cnt,
-                     float* __restrict__ rho_out, float* __restrict__ lam_out) {
+                     float* __restrict__ rho_out, float* __restrict__ lam_out,
+                     float* __restrict__ lacc) {
     const StepParams& p = *P;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = p.n;
@@ -135,7 +136,9 @@ __global__ void __launch_bounds__(128)
         acc.add2(p, xi, __ldg(ps + j0), __ldg(ps + j1), two);
     });
     rho_out[i] = acc.rho;
-    lam_out[i] = acc.lambda(p);
+    const float l = acc.lambda(p);
+    lam_out[i] = l;
+    if (lacc) lacc[i] += l;  // learned modes: the step's accumulated lambda
 }
 
 // (W(r2) / W(dq^2))^n of two pairs: the power in s_corr = -k * (...)^n (ConstraintSolverCUDA.cu:124).

@@ -49,7 +49,8 @@ __global__ void __launch_bounds__(kSearchBlock)
              const float4* __restrict__ xref, const uint2* __restrict__ table,
              const uint32_t* __restrict__ r2i, uint32_t* __restrict__ nbr,
              uint32_t* __restrict__ cnt, float* __restrict__ rho_out, float* __restrict__ lam_out,
-             uint32_t* __restrict__ flags, int density) {
+             uint32_t* __restrict__ flags, int density, float4* __restrict__ vstar,
+             float* __restrict__ lacc) {
     extern __shared__ __align__(16) uint32_t stage[];
     const StepParams& p = *P;
     const int n = p.n;
@@ -165,7 +166,12 @@ __global__ void __launch_bounds__(kSearchBlock)
                 acc.add2(p, xi, __ldg(ps + e.z), __ldg(ps + (left >= 4 ? e.w : e.z)), left >= 4);
         }
         rho_out[i] = acc.rho;
-        lam_out[i] = acc.lambda(p);
+        const float l = acc.lambda(p);
+        lam_out[i] = l;
+        if (lacc) {  // learned modes: density beside the predicted velocity; lambda sum starts
+            vstar[i].w = acc.rho;
+            lacc[i] = l;
+        }
     }
 }
 

@@ -21,7 +21,9 @@
 #include <vector>
 
 #include "akua_pbf.h"
+#include "mlp_handle.h"
 #include "pbf_kernels.cuh"
+#include "pbf_learned.cuh"
 #include "radix_sort.cuh"
 
 using akua::StepParams;
@@ -79,6 +81,19 @@ struct akua_pbf {
     int graph_captures = 0;
     int body_launches = 0;
 
+    // learned warm start (allocated on first use): features, predicted velocity (.w = density),
+    // the step's accumulated lambda, the previous step's (internal order) and the export copy
+    // (reference order, read back at import)
+    akua_mlp* warm = nullptr;
+    bool track = false;  // accumulate lambda and compute features every step
+    float* cap_feat = nullptr;
+    float* cap_target = nullptr;
+    float *feat = nullptr, *lacc = nullptr, *lprev = nullptr, *lacc_ref = nullptr;
+    float4* vs4 = nullptr;
+    uint32_t* err_max = nullptr;
+    double* err_sum = nullptr;
+    int graph_learn = 0;
+
     int64_t steps = 0;
     uint64_t device_bytes = 0;
 
@@ -89,6 +104,11 @@ struct akua_pbf {
     std::vector<const char*> prof_names;  // nullptr marks the start of a step
     size_t prof_next = 0;
 };
+
+namespace akua::mlp {
+int enqueue_forward(const akua_mlp* m, const float* feat, int n, float* out, float* out2,
+                    cudaStream_t st);
+}
 
 namespace {
 
@@ -111,7 +131,8 @@ void free_all(akua_pbf* s) {
                     s->x4g, s->col4g, s->ps0, s->ps1, s->vstar4, s->om4, s->vc4, s->dpg, s->xref,
                     s->sizeg, s->rhog, s->lamg, s->rrefg, s->mkey, s->r2i, s->blen, s->order, s->bmix,
                     s->ka0, s->va0, s->ka1, s->va1, s->kb0, s->vb0, s->kb1, s->vb1,
-                    s->sort_scratch, s->table, s->nbr, s->cnt, s->flags, s->staging};
+                    s->sort_scratch, s->table, s->nbr, s->cnt, s->flags, s->staging,
+                    s->feat, s->lacc, s->lprev, s->lacc_ref, s->vs4, s->err_max, s->err_sum};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (s->exec) cudaGraphExecDestroy(s->exec);
@@ -198,6 +219,25 @@ StepParams make_params(const akua_pbf* s, float dt, const float* bmin, const flo
 
 inline int grid_for(int n, int block) { return (n + block - 1) / block; }
 
+// 0: plain step; 1: features and accumulated lambda are tracked (training capture); 2: and the
+// network's prediction replaces iteration 1's lambda.
+int learn_mode(const akua_pbf* s) { return s->warm ? 2 : ((s->track || s->cap_feat) ? 1 : 0); }
+
+cudaError_t ensure_learn_buffers(akua_pbf* s) {
+    if (s->feat) return cudaSuccess;
+    const int n = s->n;
+    cudaError_t e = dalloc(s, &s->feat, (size_t)8 * n);
+    if (e == cudaSuccess) e = dalloc(s, &s->lacc, n);
+    if (e == cudaSuccess) e = dalloc(s, &s->lprev, n);
+    if (e == cudaSuccess) e = dalloc(s, &s->lacc_ref, n);
+    if (e == cudaSuccess) e = dalloc(s, &s->vs4, n);
+    if (e == cudaSuccess) e = dalloc(s, &s->err_max, 1);
+    if (e == cudaSuccess) e = dalloc(s, &s->err_sum, 1);
+    if (e == cudaSuccess) e = cudaMemset(s->lacc, 0, sizeof(float) * n);
+    if (e == cudaSuccess) e = cudaMemset(s->lacc_ref, 0, sizeof(float) * n);
+    return e;
+}
+
 // Counts launches and, while profiling (never during capture), records an event after each.
 struct Marker {
     akua_pbf* s;
@@ -221,11 +261,21 @@ void enqueue_pairs(akua_pbf* s, cudaStream_t st, Marker& mark) {
     const int iters = s->cfg.solverIterations;
     float4* ps[2] = {s->ps0, s->ps1};
     const uint4* nbr4 = reinterpret_cast<const uint4*>(s->nbr);
+    const int learn = learn_mode(s);
     akua::k_search<EXACT><<<grid_for(n, akua::kSearchBlock), akua::kSearchBlock,
                             akua::kSearchSmem, st>>>(
         s->d_params, s->ps0, s->xref, s->table, s->r2i, s->nbr, s->cnt, s->rho, s->lam,
-        s->flags, iters > 0 ? 1 : 0);
+        s->flags, iters > 0 ? 1 : 0, learn ? s->vs4 : nullptr, learn ? s->lacc : nullptr);
     mark("k_search");
+    if (learn) {
+        akua::k_features<<<gp, akua::kPairBlock, 0, st>>>(s->d_params, s->ps0, s->vs4, s->lam,
+                                                           s->lprev, nbr4, s->cnt, s->feat);
+        mark("k_features");
+    }
+    if (learn == 2) {
+        akua::mlp::enqueue_forward(s->warm, s->feat, n, s->lam, s->lacc, st);
+        mark("k_mlp_forward");
+    }
     akua::k_table_clear<<<grid_for(n, akua::kElemBlock), akua::kElemBlock, 0, st>>>(s->d_params,
                                                                                    s->kr, s->table);
     mark("k_table_clear");
@@ -233,8 +283,8 @@ void enqueue_pairs(akua_pbf* s, cudaStream_t st, Marker& mark) {
         float4* cur = ps[it & 1];
         float4* nxt = ps[(it + 1) & 1];
         if (it > 0) {
-            akua::k_density_lambda<EXACT><<<gp, akua::kPairBlock, 0, st>>>(s->d_params, cur, nbr4,
-                                                                           s->cnt, s->rho, s->lam);
+            akua::k_density_lambda<EXACT><<<gp, akua::kPairBlock, 0, st>>>(
+                s->d_params, cur, nbr4, s->cnt, s->rho, s->lam, learn ? s->lacc : nullptr);
             mark("k_density_lambda");
         }
         if (it + 1 < iters) {
@@ -287,7 +337,8 @@ void enqueue_body(akua_pbf* s, cudaStream_t st, const char* aos, size_t stride, 
     akua::k_gather<<<ge, akua::kElemBlock, 0, st>>>(
         s->d_params, s->spperm, s->refperm, s->x4, s->v4, s->col4, s->size, s->rref, s->x4g,
         s->col4g, s->sizeg, s->ps0, s->r2i, s->rrefg, s->xref, s->order, s->rho, s->lam, s->dp4,
-        s->rhog, s->lamg, s->dpg, carry ? 1 : 0);
+        s->rhog, s->lamg, s->dpg, carry ? 1 : 0, s->lacc, s->lprev,
+        learn_mode(s) ? s->vs4 : nullptr);
     mark("k_gather");
     akua::k_ref_table<<<ge, akua::kElemBlock, 0, st>>>(s->d_params, s->kr, s->table, s->bmix);
     mark("k_ref_table");
@@ -302,7 +353,8 @@ void enqueue_body(akua_pbf* s, cudaStream_t st, const char* aos, size_t stride, 
     if (aos) {
         akua::k_export<<<grid_for(n, akua::kIoBlock), akua::kIoBlock, 0, st>>>(
             const_cast<char*>(aos), stride, n, s->r2i, s->kr, s->x4, s->v4, s->vstar4, s->dp4,
-            s->om4, s->rho, s->lam, s->col4, s->size);
+            s->om4, s->rho, s->lam, s->col4, s->size, s->lacc,
+            learn_mode(s) ? s->lacc_ref : nullptr);
         mark("k_export");
     }
     s->body_launches = mark.launches;
@@ -324,7 +376,8 @@ void update_plans(akua_pbf* s, int sp_bits) {
 
 int ensure_graph(akua_pbf* s, const char* aos, size_t stride) {
     if (s->graph_ok && s->graph_options == s->options && s->graph_aos == aos &&
-        s->graph_stride == stride && s->graph_sp_bits == s->sp_bits)
+        s->graph_stride == stride && s->graph_sp_bits == s->sp_bits &&
+        s->graph_learn == learn_mode(s))
         return AKUA_OK;
     invalidate_graph(s);
     cudaError_t e = cudaStreamBeginCapture(s->capture_stream, cudaStreamCaptureModeThreadLocal);
@@ -345,6 +398,7 @@ int ensure_graph(akua_pbf* s, const char* aos, size_t stride) {
     s->graph_aos = aos;
     s->graph_stride = stride;
     s->graph_sp_bits = s->sp_bits;
+    s->graph_learn = learn_mode(s);
     ++s->graph_captures;
     return AKUA_OK;
 }
@@ -374,6 +428,11 @@ int do_step(akua_pbf* s, const char* aos, size_t stride, bool force_import, floa
             aos, stride, s->n, s->x4, s->v4, s->col4, s->size, s->rref, s->rho, s->lam, s->dp4,
             s->cfg.solverIterations == 0 ? 1 : 0);
         mark("k_import");
+        if (learn_mode(s)) {  // the previous step's lambda sums, in the records' order
+            cudaError_t ce = cudaMemcpyAsync(s->lacc, s->lacc_ref, sizeof(float) * s->n,
+                                             cudaMemcpyDeviceToDevice, st);
+            if (ce != cudaSuccess) return cuda_status(ce);
+        }
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_status(e);
@@ -387,6 +446,16 @@ int do_step(akua_pbf* s, const char* aos, size_t stride, bool force_import, floa
     }
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_status(e);
+    if (s->cap_feat) {  // one-shot training capture
+        e = cudaMemcpyAsync(s->cap_feat, s->feat, sizeof(float) * 8 * s->n,
+                            cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(s->cap_target, s->lacc, sizeof(float) * s->n,
+                                cudaMemcpyDeviceToDevice, st);
+        s->cap_feat = nullptr;
+        s->cap_target = nullptr;
+        if (e != cudaSuccess) return cuda_status(e);
+    }
     s->state_valid = true;
     s->stepped = true;
     ++s->steps;
@@ -562,6 +631,14 @@ int akua_pbf_set_boundary_damping(akua_pbf* s, float restitution, float friction
     return AKUA_OK;
 }
 
+int akua_pbf_set_solver_iterations(akua_pbf* s, int32_t iterations) {
+    if (!s || iterations < 0 || iterations > 1000) return AKUA_ERR_INVALID_ARGUMENT;
+    if ((s->warm || s->cap_feat || s->track) && iterations < 1) return AKUA_ERR_INVALID_ARGUMENT;
+    s->cfg.solverIterations = iterations;
+    invalidate_graph(s);
+    return AKUA_OK;
+}
+
 int akua_pbf_set_table_size(akua_pbf* s, int32_t table_size) {
     if (!s || table_size <= 0) return AKUA_ERR_INVALID_ARGUMENT;
     DeviceGuard g(s->device);
@@ -657,7 +734,7 @@ int akua_pbf_read_debug(akua_pbf* s, int32_t what, void* dst, size_t bytes) {
         }
         akua::k_export<<<grid_for(s->n, akua::kIoBlock), akua::kIoBlock, 0, s->stream>>>(
             tmp, sizeof(akua_particle), s->n, s->r2i, s->kr, s->x4, s->v4, s->vstar4, s->dp4,
-            s->om4, s->rho, s->lam, s->col4, s->size);
+            s->om4, s->rho, s->lam, s->col4, s->size, nullptr, nullptr);
         e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaMemcpyAsync(dst, tmp, need, cudaMemcpyDeviceToHost, s->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
@@ -757,6 +834,71 @@ int akua_pbf_profile_end(akua_pbf* s, akua_kernel_time* out, int32_t capacity, i
         ++k;
     }
     *count = k;
+    return AKUA_OK;
+}
+
+int akua_pbf_set_warm_start(akua_pbf* s, akua_mlp* net) {
+    if (!s) return AKUA_ERR_INVALID_ARGUMENT;
+    if (net && (net->device != s->device || s->cfg.solverIterations < 1))
+        return AKUA_ERR_INVALID_ARGUMENT;
+    DeviceGuard g(s->device);
+    if (net) {
+        const cudaError_t e = ensure_learn_buffers(s);
+        if (e != cudaSuccess) return cuda_status(e);
+    }
+    s->warm = net;
+    return AKUA_OK;
+}
+
+int akua_pbf_capture_training(akua_pbf* s, float* features, float* targets) {
+    if (!s || (!features) != (!targets)) return AKUA_ERR_INVALID_ARGUMENT;
+    if (features && s->cfg.solverIterations < 1) return AKUA_ERR_INVALID_ARGUMENT;
+    DeviceGuard g(s->device);
+    if (features) {
+        const cudaError_t e = ensure_learn_buffers(s);
+        if (e != cudaSuccess) return cuda_status(e);
+    }
+    s->cap_feat = features;
+    s->cap_target = targets;
+    if (features) s->track = true;
+    return AKUA_OK;
+}
+
+int akua_pbf_set_lambda_tracking(akua_pbf* s, int32_t enabled) {
+    if (!s) return AKUA_ERR_INVALID_ARGUMENT;
+    if (enabled && s->cfg.solverIterations < 1) return AKUA_ERR_INVALID_ARGUMENT;
+    DeviceGuard g(s->device);
+    if (enabled) {
+        const cudaError_t e = ensure_learn_buffers(s);
+        if (e != cudaSuccess) return cuda_status(e);
+    }
+    s->track = enabled != 0;
+    return AKUA_OK;
+}
+
+int akua_pbf_density_error(akua_pbf* s, float* max_error, float* mean_abs_error) {
+    if (!s || !max_error || !mean_abs_error) return AKUA_ERR_INVALID_ARGUMENT;
+    if (!s->stepped) return AKUA_ERR_NOT_ATTACHED;
+    DeviceGuard g(s->device);
+    cudaError_t e = ensure_learn_buffers(s);
+    cudaStream_t st = s->stream;
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->err_max, 0, sizeof(uint32_t), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->err_sum, 0, sizeof(double), st);
+    if (e != cudaSuccess) return cuda_status(e);
+    akua::k_density_error<<<grid_for(s->n, akua::kPairBlock), akua::kPairBlock, 0, st>>>(
+        s->d_params, s->x4, reinterpret_cast<const uint4*>(s->nbr), s->cnt, s->err_max,
+        s->err_sum);
+    uint32_t bits = 0;
+    double sum = 0.0;
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&bits, s->err_max, sizeof(bits), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&sum, s->err_sum, sizeof(sum), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_status(e);
+    float m;
+    std::memcpy(&m, &bits, sizeof(m));
+    *max_error = m;
+    *mean_abs_error = (float)(sum / (double)s->n);
     return AKUA_OK;
 }
 

@@ -138,6 +138,45 @@ class PBFSolver:
                                            PARTICLE_DTYPE.itemsize, float(deltaTime),
                                            vec3(boxMin), vec3(boxMax)), "akua_pbf_step_host")
 
+    def set_solver_iterations(self, iterations: int) -> None:
+        check(self._lib.akua_pbf_set_solver_iterations(self._h, int(iterations)),
+              "akua_pbf_set_solver_iterations")
+        self.config.solverIterations = int(iterations)
+
+    def set_warm_start(self, net) -> None:
+        """Attaches a LambdaNet (None: the plain solver)."""
+        check(self._lib.akua_pbf_set_warm_start(self._h, net.handle if net is not None else None),
+              "akua_pbf_set_warm_start")
+        self._warm = net
+
+    def capture_training(self, features, targets) -> None:
+        """The next step writes features (CUDA float32 [N, 8]) and accumulated lambda (CUDA
+        float32 [N]) in one particle order."""
+        if features is None:
+            check(self._lib.akua_pbf_capture_training(self._h, None, None), "capture_training")
+            return
+        n = self.numParticles
+        if tuple(features.shape) != (n, 8) or tuple(targets.shape) != (n,):
+            raise ValueError("expected features [%d, 8] and targets [%d]" % (n, n))
+        for t in (features, targets):
+            if not t.is_cuda or not t.is_contiguous() or str(t.dtype) != "torch.float32":
+                raise ValueError("capture buffers must be contiguous CUDA float32 tensors")
+        check(self._lib.akua_pbf_capture_training(self._h, ctypes.c_void_p(features.data_ptr()),
+                                                  ctypes.c_void_p(targets.data_ptr())),
+              "akua_pbf_capture_training")
+        self._capture = (features, targets)
+
+    def set_lambda_tracking(self, enabled: bool) -> None:
+        check(self._lib.akua_pbf_set_lambda_tracking(self._h, int(bool(enabled))),
+              "akua_pbf_set_lambda_tracking")
+
+    def density_error(self) -> tuple[float, float]:
+        """(max_i max(rho_i/rho0 - 1, 0), mean_i |rho_i/rho0 - 1|) at the last step's end."""
+        mx, mean = ctypes.c_float(), ctypes.c_float()
+        check(self._lib.akua_pbf_density_error(self._h, ctypes.byref(mx), ctypes.byref(mean)),
+              "akua_pbf_density_error")
+        return float(mx.value), float(mean.value)
+
     def set_options(self, options: int) -> None:
         check(self._lib.akua_pbf_set_options(self._h, int(options)), "akua_pbf_set_options")
 

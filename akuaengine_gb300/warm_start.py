@@ -1,0 +1,268 @@
+"""Learned lambda warm start: the network handle, training-pair collection and training.
+
+The network (C ABI `akua_mlp_*`, tensor-core kernels in csrc/mlp.cuh) predicts, from eight
+features of a particle at the start of a step, the lambda that a long plain solve accumulates
+over that step.  A solver with the network attached (`PBFSolver.set_warm_start`) uses the
+prediction in its first Jacobi iteration and runs its remaining iterations unchanged; the plain
+iterated solver stays the fallback (detach the network) and `PBFSolver.density_error` judges both.
+
+Training pairs come from the solver itself: a "teacher" solver runs the scene with many
+iterations (20 by default) and `capture_training` records, every few steps, the features at the
+start of the step and the lambda the step accumulated.  Training runs the network's own forward
+and backward kernels with Adam on the GPU; torch is used only to hold device buffers and to
+shuffle and slice them.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _abi
+from ._abi import MLP_NORM, MLP_PARAMS, check, load_library
+
+PARAM_SHAPES = [("W1", (64, 8)), ("b1", (64,)), ("W2", (64, 64)), ("b2", (64,)),
+                ("W3", (64, 64)), ("b3", (64,)), ("w4", (64,)), ("b4", (1,))]
+FEATURE_NAMES = ["density_constraint", "neighbours_over_32", "lambda_denominator",
+                 "lambda_iteration_1", "previous_lambda_sum", "mean_neighbour_constraint",
+                 "velocity_divergence", "speed"]
+
+
+def init_params(seed: int = 0) -> np.ndarray:
+    """Uniform(+-sqrt(6 / (fan_in + fan_out))) weights, zero biases, a small output layer."""
+    rng = np.random.default_rng(seed)
+    parts = []
+    for name, shape in PARAM_SHAPES:
+        if name.startswith("b"):
+            parts.append(np.zeros(shape))
+        elif name == "w4":
+            parts.append(rng.uniform(-1, 1, shape) * np.sqrt(6.0 / 65.0) * 0.5)
+        else:
+            fan_out, fan_in = shape
+            parts.append(rng.uniform(-1, 1, shape) * np.sqrt(6.0 / (fan_in + fan_out)))
+    return np.concatenate([p.reshape(-1) for p in parts]).astype(np.float32)
+
+
+class LambdaNet:
+    """The network on the current CUDA device."""
+
+    def __init__(self, params: np.ndarray | None = None, seed: int = 0):
+        self._lib = load_library()
+        h = ctypes.c_void_p()
+        check(self._lib.akua_mlp_create(ctypes.byref(h)), "akua_mlp_create")
+        self._h = h
+        self.norm = np.concatenate([np.zeros(8), np.ones(8), [1.0]]).astype(np.float32)
+        self.out_scale = 1.0  # lambda units of one network output unit, as trained
+        self.gain = 1.0       # multiplier applied when the prediction is used in a step
+        self.set_params(init_params(seed) if params is None else params)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_params(self, params) -> None:
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        if p.size != MLP_PARAMS:
+            raise ValueError("expected %d parameters" % MLP_PARAMS)
+        check(self._lib.akua_mlp_set_params(self._h, p.ctypes.data_as(ctypes.c_void_p), p.size),
+              "akua_mlp_set_params")
+
+    def params(self) -> np.ndarray:
+        p = np.zeros(MLP_PARAMS, dtype=np.float32)
+        check(self._lib.akua_mlp_get_params(self._h, p.ctypes.data_as(ctypes.c_void_p), p.size),
+              "akua_mlp_get_params")
+        return p
+
+    def set_normalization(self, mean, inv_std, out_scale: float) -> None:
+        norm = np.concatenate([np.asarray(mean, np.float32).reshape(8),
+                               np.asarray(inv_std, np.float32).reshape(8),
+                               [np.float32(out_scale)]]).astype(np.float32)
+        check(self._lib.akua_mlp_set_normalization(self._h, norm.ctypes.data_as(ctypes.c_void_p),
+                                                   MLP_NORM), "akua_mlp_set_normalization")
+        self.norm = norm
+        self.out_scale = float(out_scale)
+        self.gain = 1.0
+
+    def set_gain(self, gain: float) -> None:
+        """Scales the prediction the step uses (the trained output scale times `gain`).  Set it
+        after training: the loss is defined on the scaled output."""
+        scale, mean, inv = self.out_scale, self.norm[:8].copy(), self.norm[8:16].copy()
+        self.set_normalization(mean, inv, scale * float(gain))
+        self.out_scale = scale
+        self.gain = float(gain)
+
+    def fit_normalization(self, features, targets) -> None:
+        """Per-feature mean and 1/std, and the targets' standard deviation as output scale."""
+        import torch
+
+        f = features.double()
+        mean = f.mean(0)
+        std = f.std(0)
+        inv = torch.where(std > 1e-30, 1.0 / std.clamp_min(1e-30), torch.ones_like(std))
+        scale = float(targets.double().std())
+        if not scale > 0:
+            scale = 1.0
+        self.set_normalization(mean.cpu().numpy(), inv.cpu().numpy(), scale)
+
+    def forward(self, features, out=None, stream=None):
+        import torch
+
+        n = features.shape[0]
+        if out is None:
+            out = torch.empty(n, dtype=torch.float32, device=features.device)
+        _check_tensor(features, (n, 8))
+        _check_tensor(out, (n,))
+        check(self._lib.akua_mlp_forward(self._h, _ptr(features), _ptr(out), n, _stream(stream)),
+              "akua_mlp_forward")
+        return out
+
+    def gradient(self, features, targets, stream=None) -> tuple[np.ndarray, float]:
+        n = features.shape[0]
+        _check_tensor(features, (n, 8))
+        _check_tensor(targets, (n,))
+        g = np.zeros(MLP_PARAMS, dtype=np.float32)
+        loss = ctypes.c_float()
+        check(self._lib.akua_mlp_gradient(self._h, _ptr(features), _ptr(targets), n,
+                                          g.ctypes.data_as(ctypes.c_void_p), ctypes.byref(loss),
+                                          _stream(stream)), "akua_mlp_gradient")
+        return g, float(loss.value)
+
+    def adam_step(self, features, targets, lr: float, stream=None) -> None:
+        n = features.shape[0]
+        check(self._lib.akua_mlp_adam_step(self._h, _ptr(features), _ptr(targets), n, float(lr),
+                                           _stream(stream)), "akua_mlp_adam_step")
+
+    def synchronize(self, stream=None) -> None:
+        check(self._lib.akua_mlp_synchronize(self._h, _stream(stream)), "akua_mlp_synchronize")
+
+    def save(self, path: str) -> None:
+        np.savez(path, params=self.params(), norm=self.norm, out_scale=self.out_scale,
+                 gain=self.gain)
+
+    @classmethod
+    def load(cls, path: str) -> "LambdaNet":
+        d = np.load(path)
+        net = cls(params=d["params"])
+        norm = d["norm"]
+        net.set_normalization(norm[:8], norm[8:16], float(d["out_scale"]))
+        net.set_gain(float(d["gain"]))
+        return net
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            rc = self._lib.akua_mlp_destroy(self._h)
+            self._h = ctypes.c_void_p()
+            check(rc, "akua_mlp_destroy")
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _stream(stream):
+    if stream is None:
+        return None
+    return ctypes.c_void_p(int(getattr(stream, "cuda_stream", stream)))
+
+
+def _check_tensor(t, shape):
+    if (not t.is_cuda or not t.is_contiguous() or str(t.dtype) != "torch.float32"
+            or tuple(t.shape) != tuple(shape)):
+        raise ValueError("expected a contiguous CUDA float32 tensor of shape %s" % (shape,))
+
+
+def collect_pairs(sc, cfg, corr, steps: int, capture_every: int, first_capture: int = 2,
+                  teacher_iterations: int = 20, stream=None):
+    """Steps scene `sc` with a `teacher_iterations` solver for `steps` steps and returns the
+    (features [M, 8], targets [M]) pairs captured every `capture_every` steps from step
+    `first_capture` on (the first steps have no previous lambda sum to report)."""
+    import torch
+
+    from .solver import PBFConfig, PBFSolver
+
+    tcfg = PBFConfig(**{**cfg.__dict__, "solverIterations": int(teacher_iterations)})
+    solver = PBFSolver(sc.n, tcfg, corr, stream=stream)
+    solver.set_lambda_tracking(True)
+    buf = torch.from_numpy(sc.particles.view(np.uint8).copy()).cuda()
+    feats, targs = [], []
+    try:
+        for k in range(steps):
+            if k >= first_capture and (k - first_capture) % capture_every == 0:
+                f = torch.empty((sc.n, 8), dtype=torch.float32, device="cuda")
+                t = torch.empty(sc.n, dtype=torch.float32, device="cuda")
+                solver.capture_training(f, t)
+                feats.append(f)
+                targs.append(t)
+            solver.step(buf, sc.dt, sc.box_min, sc.box_max)
+        solver.synchronize()
+    finally:
+        solver.close()
+    return torch.cat(feats), torch.cat(targs)
+
+
+def train(net: LambdaNet, features, targets, epochs: int = 8, batch: int = 65536,
+          lr: float = 2e-3, lr_final: float = 2e-4, seed: int = 0, stream=None) -> list[float]:
+    """Adam over shuffled minibatches with a geometric learning-rate decay; returns the loss on
+    the whole set after each epoch (one gradient pass)."""
+    import torch
+
+    n = features.shape[0]
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    per_epoch = max(1, (n + batch - 1) // batch)
+    total = epochs * per_epoch
+    losses = []
+    k = 0
+    for _ in range(epochs):
+        perm = torch.randperm(n, generator=g).to(features.device)
+        xf, yf = features[perm].contiguous(), targets[perm].contiguous()
+        for b0 in range(0, n, batch):
+            rate = lr * (lr_final / lr) ** (k / max(total - 1, 1))
+            net.adam_step(xf[b0:b0 + batch], yf[b0:b0 + batch], rate, stream)
+            k += 1
+        net.synchronize(stream)
+        losses.append(net.gradient(features, targets, stream)[1])
+    return losses
+
+
+def rollout_errors(sc, cfg, corr, iterations: int, net=None, steps: int = 60, stream=None):
+    """Density-constraint errors [(max C, mean |C|) per step] of `steps` steps of scene `sc` with
+    `iterations` Jacobi iterations, warm-started by `net` when given."""
+    import torch
+
+    from .solver import PBFSolver
+
+    s = PBFSolver(sc.n, cfg, corr, stream=stream)
+    s.set_solver_iterations(iterations)
+    if net is not None:
+        s.set_warm_start(net)
+    buf = torch.from_numpy(sc.particles.view(np.uint8).copy()).cuda()
+    errs = []
+    try:
+        for _ in range(steps):
+            s.step(buf, sc.dt, sc.box_min, sc.box_max)
+            errs.append(s.density_error())
+    finally:
+        s.close()
+    return np.array(errs)
+
+
+def calibrate_gain(net: LambdaNet, sc, cfg, corr, iterations: int,
+                   gains=(0.3, 0.4, 0.5, 0.6, 0.75), steps: int = 60, stream=None) -> dict:
+    """Picks the gain whose rollout of `sc` has the lowest mean |C| (max C breaks ties) and sets
+    it; returns {gain: (mean of max C, mean of mean |C|)}."""
+    res = {}
+    for g in gains:
+        net.set_gain(g)
+        e = rollout_errors(sc, cfg, corr, iterations, net, steps, stream)
+        bad = not np.isfinite(e).all()
+        res[float(g)] = (float("inf"), float("inf")) if bad else (float(e[:, 0].mean()),
+                                                                  float(e[:, 1].mean()))
+    best = min(res, key=lambda g: (res[g][1], res[g][0]))
+    net.set_gain(best)
+    return res

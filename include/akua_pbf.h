@@ -138,6 +138,9 @@ int akua_pbf_set_boundary_damping(akua_pbf* solver, float restitution, float fri
  * Changing it changes every hash, hence the sorted order. */
 int akua_pbf_set_table_size(akua_pbf* solver, int32_t tableSize);
 
+/* New: PBFConfig::solverIterations after construction (the reference fixes it when the solver is
+ * built, PBFSolver.cpp:13-20); 0 .. 1000. */
+int akua_pbf_set_solver_iterations(akua_pbf* solver, int32_t iterations);
 /* New: the CUDA stream (a cudaStream_t) all device work of this handle is issued on. */
 int akua_pbf_set_stream(akua_pbf* solver, void* cudaStream);
 
@@ -182,6 +185,60 @@ int akua_pbf_profile_end(akua_pbf* solver, akua_kernel_time* out, int32_t capaci
 #define AKUA_SORT_NOALLOC_MAX_PAIRS (1 << 20)
 int akua_sort_pairs_noalloc(const uint32_t* keysIn, const uint32_t* valsIn, uint32_t* keysOut,
                             uint32_t* valsOut, int32_t n, int32_t keyBits, void* cudaStream);
+
+/* ---- Learned lambda warm start.  No counterpart in the reference. ----------------------------
+ * A network of 8 inputs, three hidden layers of 64 SiLU units and one output, BF16 weights and
+ * activations on the tensor cores with FP32 accumulation, trained on the GPU.  It predicts, from
+ * per-particle features at the start of a step, the lambda a 20-iteration solve accumulates over
+ * the step; with a network attached, a step's first Jacobi iteration uses that prediction instead
+ * of the one-step estimate and the remaining iterations run unchanged.
+ * Features (float[8] per particle): rho/rho0 - 1, neighbours / 32, the lambda denominator without
+ * epsilon, iteration 1's lambda, the previous step's accumulated lambda, the mean rho_j/rho0 - 1
+ * of the neighbours, the SPH divergence of the predicted velocity, |predicted velocity|.
+ * Parameters (float[AKUA_MLP_PARAMS], FP32 master copy): W1[64][8], b1[64], W2[64][64], b2[64],
+ * W3[64][64], b3[64], w4[64], b4.  Normalisation (float[AKUA_MLP_NORM]): mean[8], inv_std[8] of
+ * the features, and the output scale (the network's output times it is lambda). */
+#define AKUA_MLP_INPUTS 8
+#define AKUA_MLP_HIDDEN 64
+#define AKUA_MLP_PARAMS 8961
+#define AKUA_MLP_NORM 17
+typedef struct akua_mlp akua_mlp;
+/* Allocates the network on the current device (zero parameters, identity normalisation). */
+int akua_mlp_create(akua_mlp** out);
+int akua_mlp_destroy(akua_mlp* net);
+/* Host copies of the FP32 parameters; setting them resets the optimiser state.  Synchronous. */
+int akua_mlp_set_params(akua_mlp* net, const float* hostParams, int32_t count);
+int akua_mlp_get_params(akua_mlp* net, float* hostParams, int32_t count);
+int akua_mlp_set_normalization(akua_mlp* net, const float* hostNorm, int32_t count);
+/* out[i] = network(features[8 i .. 8 i + 7]) for n particles (device arrays); asynchronous. */
+int akua_mlp_forward(akua_mlp* net, const float* deviceFeatures, float* deviceOut, int32_t n,
+                     void* cudaStream);
+/* Gradient of L = (1/n) sum_i (out_i - target_i)^2 / outScale^2 with respect to the FP32
+ * parameters (hostGrad[AKUA_MLP_PARAMS], may be NULL) and L itself (hostLoss, may be NULL);
+ * synchronous.  Returns AKUA_ERR_DEVICE_CHECK if a tensor-core wait timed out. */
+int akua_mlp_gradient(akua_mlp* net, const float* deviceFeatures, const float* deviceTargets,
+                      int32_t n, float* hostGrad, float* hostLoss, void* cudaStream);
+/* One Adam step (beta 0.9 / 0.999, eps 1e-8) on L over the n given samples; asynchronous. */
+int akua_mlp_adam_step(akua_mlp* net, const float* deviceFeatures, const float* deviceTargets,
+                       int32_t n, float learningRate, void* cudaStream);
+/* Waits for the stream; AKUA_ERR_DEVICE_CHECK if any kernel of the network reported a timeout. */
+int akua_mlp_synchronize(akua_mlp* net, void* cudaStream);
+/* Attaches a network (NULL detaches: the plain solver) to a solver on the same device.  Needs
+ * solverIterations >= 1.  The network must outlive the attachment. */
+int akua_pbf_set_warm_start(akua_pbf* solver, akua_mlp* net);
+/* Makes the next step write, in one consistent particle order, the features of every particle at
+ * its start (deviceFeatures, float[8 N]) and the lambda its iterations accumulated
+ * (deviceTargets, float[N]): training pairs when the step runs a long plain solve.  NULLs cancel.
+ * Needs solverIterations >= 1. */
+int akua_pbf_capture_training(akua_pbf* solver, float* deviceFeatures, float* deviceTargets);
+/* Keeps the per-particle lambda sum of every step (and the features) even without a capture or a
+ * network, so that the "previous step's accumulated lambda" feature is valid at any step; a
+ * capture turns it on.  Needs solverIterations >= 1. */
+int akua_pbf_set_lambda_tracking(akua_pbf* solver, int32_t enabled);
+/* Density-constraint error of the last step: C_i = rho_i / rho0 - 1 at the positions the step
+ * ended with, over that step's neighbour lists; *maxError = max_i max(C_i, 0),
+ * *meanAbsError = mean_i |C_i|.  Synchronous. */
+int akua_pbf_density_error(akua_pbf* solver, float* maxError, float* meanAbsError);
 
 const char* akua_pbf_status_string(int status);
 int akua_pbf_abi_version(void);

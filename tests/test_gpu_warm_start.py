@@ -1,0 +1,107 @@
+"""Learned lambda warm start in the step: training-pair capture, training on the GPU with the
+network's own kernels, and what the trained network gains over the plain solver at the same
+number of Jacobi iterations (density-constraint error measured by the solver)."""
+import numpy as np
+import pytest
+
+import akuaengine_gb300 as ak
+from akuaengine_gb300 import PBFSolver, scene
+
+pytestmark = pytest.mark.gpu
+
+
+def _solver(sc, iterations, net=None):
+    import torch
+
+    cfg, corr = scene.benchmark_params()
+    s = PBFSolver(sc.n, cfg, corr)
+    s.set_solver_iterations(iterations)
+    if net is not None:
+        s.set_warm_start(net)
+    buf = torch.from_numpy(sc.particles.view(np.uint8).copy()).cuda()
+    return s, buf
+
+
+def test_capture_invariants(cuda_lib):
+    """One iteration: the accumulated lambda is iteration 1's lambda (feature 3); feature 1 is
+    the neighbour count; feature 0 the constraint of the step's density; feature 4 is the
+    previous step's accumulated lambda."""
+    import torch
+
+    sc = scene.workload("dam_break_27k", seed=4)
+    s, buf = _solver(sc, 1)
+    for _ in range(3):
+        s.step(buf, sc.dt, sc.box_min, sc.box_max)
+    caps = []
+    for _ in range(2):
+        f = torch.empty((sc.n, 8), dtype=torch.float32, device="cuda")
+        t = torch.empty(sc.n, dtype=torch.float32, device="cuda")
+        s.capture_training(f, t)
+        s.step(buf, sc.dt, sc.box_min, sc.box_max)
+        s.synchronize()
+        caps.append((f.cpu().numpy(), t.cpu().numpy()))
+    (f0, t0), (f1, t1) = caps
+    assert np.array_equal(t1, f1[:, 3])
+    counts = s.read_debug(ak.DEBUG_NEIGHBOUR_COUNTS)
+    assert np.array_equal(np.sort(np.rint(f1[:, 1] * 32).astype(np.int64)), np.sort(counts))
+    rec = s.read_debug(ak.DEBUG_PARTICLES)
+    c = rec["density"] * np.float32(1.0 / 7600.0) - np.float32(1.0)
+    assert np.allclose(np.sort(f1[:, 0]), np.sort(c), atol=1e-6)
+    assert np.array_equal(np.sort(f1[:, 4]), np.sort(t0))
+    assert np.isfinite(f1).all() and np.isfinite(t1).all()
+    s.close()
+
+
+@pytest.fixture(scope="module")
+def trained(cuda_lib):
+    from akuaengine_gb300.warm_start import LambdaNet, calibrate_gain, collect_pairs, train
+
+    sc = scene.workload("dam_break_27k", seed=0)
+    cfg, corr = scene.benchmark_params()
+    x, y = collect_pairs(sc, cfg, corr, steps=90, capture_every=3, first_capture=2)
+    net = LambdaNet(seed=0)
+    net.fit_normalization(x, y)
+    _, loss0 = net.gradient(x, y)
+    losses = train(net, x, y, epochs=25, batch=16384)
+    cal = calibrate_gain(net, sc, cfg, corr, iterations=2, steps=60)
+    yield net, loss0, losses, int(x.shape[0]), cal
+    net.close()
+
+
+def test_training_reduces_loss(trained):
+    net, loss0, losses, pairs, cal = trained
+    print("pairs %d, loss %.4g -> %s" % (pairs, loss0, ["%.4g" % v for v in losses]))
+    print("gain calibration (iterations 2): %s -> %.2f" % (cal, net.gain))
+    assert losses[-1] < 0.1 * loss0
+
+
+def test_warm_start_gains_over_plain_solver(trained):
+    """On a scene the network was not trained on: two iterations warm-started beat two plain
+    iterations in both the mean and the max density-constraint error."""
+    from akuaengine_gb300.warm_start import rollout_errors
+
+    net = trained[0]
+    sc = scene.workload("dam_break_27k", seed=1)
+    cfg, corr = scene.benchmark_params()
+    steps = 90
+    res = {}
+    for name, it, use in (("plain1", 1, False), ("plain2", 2, False), ("warm2", 2, True),
+                          ("plain4", 4, False)):
+        e = rollout_errors(sc, cfg, corr, it, net if use else None, steps)
+        res[name] = e
+        print("%-7s max C %.5f (worst %.5f)  mean |C| %.5f"
+              % (name, e[:, 0].mean(), e[:, 0].max(), e[:, 1].mean()))
+    assert res["warm2"][:, 1].mean() < res["plain2"][:, 1].mean()
+    assert res["warm2"][:, 0].mean() < res["plain2"][:, 0].mean()
+
+
+def test_warm_start_launches_features_and_network(trained):
+    net = trained[0]
+    sc = scene.workload("dam_break_27k", seed=2)
+    counts = []
+    for use in (False, True):
+        s, buf = _solver(sc, 2, net if use else None)
+        s.step(buf, sc.dt, sc.box_min, sc.box_max)
+        counts.append(s.kernels_per_step())
+        s.close()
+    assert counts[1] == counts[0] + 2
