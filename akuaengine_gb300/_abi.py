@@ -25,7 +25,7 @@ OPT_NO_GRAPH = 0x4
 MLP_INPUTS = 8
 MLP_HIDDEN = 64
 MLP_PARAMS = 8961
-MLP_NORM = 17
+MLP_NORM = 18
 
 DEBUG_HASHES = 1
 DEBUG_ORDER = 2

@@ -56,7 +56,7 @@ namespace akua::mlp {
 int enqueue_forward(const akua_mlp* m, const float* feat, int n, float* out, float* out2,
                     cudaStream_t st) {
     const int tiles = (n + kTile - 1) / kTile;
-    const int grid = std::max(1, std::min(tiles, 4 * m->sms));
+    const int grid = std::max(1, std::min(tiles, 5 * m->sms));  // 5 x 40 KB of shared memory
     k_mlp_forward<<<grid, kThreads, 0, st>>>(m->params, m->norm, feat, n, out, out2, m->err);
     return status_of(cudaGetLastError());
 }
@@ -91,6 +91,7 @@ int akua_mlp_create(akua_mlp** out) {
             norm[akua::mlp::kIn + k] = 1.0f;
         }
         norm[2 * akua::mlp::kIn] = 1.0f;
+        norm[2 * akua::mlp::kIn + 1] = 1.0f;
         e = cudaMemcpy(m->norm, norm, sizeof(norm), cudaMemcpyHostToDevice);
     }
     if (e != cudaSuccess) {

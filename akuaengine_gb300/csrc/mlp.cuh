@@ -45,12 +45,20 @@ constexpr int kB3 = kW3 + kHid * kHid;  // [64]
 constexpr int kW4 = kB3 + kHid;         // [64]
 constexpr int kB4 = kW4 + kHid;         // [1]
 constexpr int kParams = kB4 + 1;        // 8961
-// Normalisation: mean[8], inv_std[8], out_scale.
-constexpr int kNorm = 2 * kIn + 1;
+// Normalisation: mean[8], inv_std[8], out_scale, blend (see k_mlp_forward).
+constexpr int kNorm = 2 * kIn + 2;
+constexpr int kLam0 = 3;  // input feature holding iteration 1's lambda
 
 constexpr int kErrTimeout = 1;
 
-__device__ __forceinline__ float sigmoid(float z) { return 1.0f / (1.0f + __expf(-z)); }
+// sigmoid(z) = (1 + tanh(z / 2)) / 2 through the hardware tanh approximation (PTX tanh.approx,
+// relative error about 2^-11); training and inference use the same forms.
+__device__ __forceinline__ float tanh_hw(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float sigmoid(float z) { return __fmaf_rn(0.5f, tanh_hw(0.5f * z), 0.5f); }
 __device__ __forceinline__ float silu(float z) { return z * sigmoid(z); }
 __device__ __forceinline__ float dsilu(float z) {
     const float s = sigmoid(z);
@@ -121,17 +129,54 @@ struct FwdSmem {
 // Epilogue of a hidden layer: TMEM columns [col, col+64) of this thread's row -> bias, SiLU,
 // BF16 -> row t of the next layer's A tile.
 __device__ __forceinline__ void hidden_epilogue(uint32_t taddr, const float* b, uint8_t* h, int t) {
-#pragma unroll 1
-    for (int c0 = 0; c0 < kHid; c0 += 16) {
-        float v[16];
-        tc::tmem_ld16(taddr + c0, v);
+    uint32_t r[4][16];
 #pragma unroll
-        for (int q = 0; q < 16; ++q) v[q] = silu(v[q] + b[c0 + q]);
-        store_row64(h, t, v, c0);
+    for (int c = 0; c < 4; ++c) tc::tmem_ld16_async(taddr + 16 * c, r[c]);
+    tc::tmem_wait_ld();
+#pragma unroll
+    for (int c = 0; c < 4; ++c) tc::tmem_after_wait(r[c]);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        float v[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) v[q] = silu(__uint_as_float(r[c][q]) + b[16 * c + q]);
+        store_row64(h, t, v, 16 * c);
     }
 }
 
-// Writes features (n x 8, FP32) -> lambda estimates out[i] (and out2[i] when given).
+// Output layer on the FP32 pipe: b4 + sum_c w4[c] silu(z3[c] + b3[c]).
+__device__ __forceinline__ float output_layer(uint32_t taddr, const float* b3, const float* w4,
+                                              float b4) {
+    uint32_t r[4][16];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) tc::tmem_ld16_async(taddr + 16 * c, r[c]);
+    tc::tmem_wait_ld();
+#pragma unroll
+    for (int c = 0; c < 4; ++c) tc::tmem_after_wait(r[c]);
+    float y = b4;
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+        for (int q = 0; q < 16; ++q)
+            y = __fmaf_rn(w4[16 * c + q], silu(__uint_as_float(r[c][q]) + b3[16 * c + q]), y);
+    return y;
+}
+
+__device__ __forceinline__ void load_features(const float* __restrict__ feat, int i, int n,
+                                              const float* norm, float (&f)[kIn]) {
+    if (i < n) {
+        const float4 a = __ldg(reinterpret_cast<const float4*>(feat) + 2 * (size_t)i);
+        const float4 b = __ldg(reinterpret_cast<const float4*>(feat) + 2 * (size_t)i + 1);
+        f[0] = a.x; f[1] = a.y; f[2] = a.z; f[3] = a.w;
+        f[4] = b.x; f[5] = b.y; f[6] = b.z; f[7] = b.w;
+    } else {
+#pragma unroll
+        for (int k = 0; k < kIn; ++k) f[k] = norm[k];
+    }
+}
+
+// Features (n x 8, FP32) -> out2[i] = the network's estimate p_i (output * out_scale) and
+// out[i] = lambda0_i + blend * (p_i - lambda0_i), lambda0 = feature 3 (blend 1: out = p).
 __global__ void __launch_bounds__(kThreads)
     k_mlp_forward(const float* __restrict__ params, const float* __restrict__ norm,
                   const float* __restrict__ feat, int n, float* __restrict__ out,
@@ -167,20 +212,17 @@ __global__ void __launch_bounds__(kThreads)
     uint32_t phase = 0;
     bool ok = true;
     const int tiles = (n + kTile - 1) / kTile;
+    float fnext[kIn];
+    load_features(feat, blockIdx.x * kTile + t, n, S.norm, fnext);
+    const float blend = S.norm[2 * kIn + 1];
     for (int tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
         const int i = tile * kTile + t;
+        const float lam0 = fnext[kLam0];
         float f[kIn];
-        if (i < n) {
-            const float4 a = reinterpret_cast<const float4*>(feat)[2 * (size_t)i];
-            const float4 b = reinterpret_cast<const float4*>(feat)[2 * (size_t)i + 1];
-            f[0] = a.x; f[1] = a.y; f[2] = a.z; f[3] = a.w;
-            f[4] = b.x; f[5] = b.y; f[6] = b.z; f[7] = b.w;
-        } else {
 #pragma unroll
-            for (int k = 0; k < kIn; ++k) f[k] = S.norm[k];
-        }
-#pragma unroll
-        for (int k = 0; k < kIn; ++k) f[k] = (f[k] - S.norm[k]) * S.norm[kIn + k];
+        for (int k = 0; k < kIn; ++k) f[k] = (fnext[k] - S.norm[k]) * S.norm[kIn + k];
+        if (tile + (int)gridDim.x < tiles)  // the next tile's features, in flight meanwhile
+            load_features(feat, (tile + gridDim.x) * kTile + t, n, S.norm, fnext);
         *reinterpret_cast<uint4*>(S.x + tc::kmajor_offset(t, 0, kInPad)) =
             make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]), pack_bf16(f[4], f[5]),
                        pack_bf16(f[6], f[7]));
@@ -219,18 +261,10 @@ __global__ void __launch_bounds__(kThreads)
             if (layer == 0) hidden_epilogue(lane, S.b2, S.h, t);
         }
         if (!ok) break;
-        // output layer on the FP32 pipe
-        float y = S.b4;
-#pragma unroll 1
-        for (int c0 = 0; c0 < kHid; c0 += 16) {
-            float v[16];
-            tc::tmem_ld16(lane + c0, v);
-#pragma unroll
-            for (int q = 0; q < 16; ++q) y = __fmaf_rn(S.w4[c0 + q], silu(v[q] + S.b3[c0 + q]), y);
-        }
+        const float y = output_layer(lane, S.b3, S.w4, S.b4);
         if (i < n) {
             const float o = y * S.norm[2 * kIn];
-            out[i] = o;
+            out[i] = blend == 1.0f ? o : __fmaf_rn(blend, o - lam0, lam0);
             if (out2) out2[i] = o;
         }
         tc::fence_before_sync();

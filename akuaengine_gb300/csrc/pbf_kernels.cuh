@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(kElemBlock)
              const float4* __restrict__ dp_in, float* __restrict__ rho_out,
              float* __restrict__ lam_out, float4* __restrict__ dp_out, int carry,
              const float* __restrict__ lacc_src, float* __restrict__ lprev_out,
-             float4* __restrict__ vstar_out) {
+             float* __restrict__ speed_out) {
     const StepParams& p = *P;
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= p.n) return;
@@ -174,10 +174,11 @@ __global__ void __launch_bounds__(kElemBlock)
     const float4 x = x4[o];
     const float4 v = v4[o];
     const float3 xs = predict(p, x, v);
-    if (vstar_out) {  // learned modes: predicted velocity and last step's accumulated lambda
-        vstar_out[s] = make_float4(__fmaf_rn(p.gravity[0], p.dt, v.x),
-                                   __fmaf_rn(p.gravity[1], p.dt, v.y),
-                                   __fmaf_rn(p.gravity[2], p.dt, v.z), 0.f);
+    if (speed_out) {  // learned modes: |predicted velocity| and last step's accumulated lambda
+        const float vx = __fmaf_rn(p.gravity[0], p.dt, v.x);
+        const float vy = __fmaf_rn(p.gravity[1], p.dt, v.y);
+        const float vz = __fmaf_rn(p.gravity[2], p.dt, v.z);
+        speed_out[s] = sqrtf(vx * vx + vy * vy + vz * vz);
         lprev_out[s] = lacc_src[o];
     }
     const float4 q = make_float4(xs.x, xs.y, xs.z, x.w);

@@ -31,6 +31,7 @@
 #include <cuda_runtime.h>
 
 #include "pbf_device.cuh"
+#include "pbf_learned.cuh"
 #include "pbf_pairs.cuh"
 
 namespace akua {
@@ -49,8 +50,9 @@ __global__ void __launch_bounds__(kSearchBlock)
              const float4* __restrict__ xref, const uint2* __restrict__ table,
              const uint32_t* __restrict__ r2i, uint32_t* __restrict__ nbr,
              uint32_t* __restrict__ cnt, float* __restrict__ rho_out, float* __restrict__ lam_out,
-             uint32_t* __restrict__ flags, int density, float4* __restrict__ vstar,
-             float* __restrict__ lacc) {
+             uint32_t* __restrict__ flags, int density, const float* __restrict__ speed,
+             const float* __restrict__ lprev, float* __restrict__ lacc,
+             float* __restrict__ feat) {
     extern __shared__ __align__(16) uint32_t stage[];
     const StepParams& p = *P;
     const int n = p.n;
@@ -168,9 +170,9 @@ __global__ void __launch_bounds__(kSearchBlock)
         rho_out[i] = acc.rho;
         const float l = acc.lambda(p);
         lam_out[i] = l;
-        if (lacc) {  // learned modes: density beside the predicted velocity; lambda sum starts
-            vstar[i].w = acc.rho;
+        if (feat) {  // learned modes: the lambda sum starts; the network's features
             lacc[i] = l;
+            write_features(p, acc, l, count, lprev[i], speed[i], feat + (size_t)kFeatures * i);
         }
     }
 }

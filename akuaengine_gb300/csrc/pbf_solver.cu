@@ -89,7 +89,7 @@ struct akua_pbf {
     float* cap_feat = nullptr;
     float* cap_target = nullptr;
     float *feat = nullptr, *lacc = nullptr, *lprev = nullptr, *lacc_ref = nullptr;
-    float4* vs4 = nullptr;
+    float* speed = nullptr;
     uint32_t* err_max = nullptr;
     double* err_sum = nullptr;
     int graph_learn = 0;
@@ -132,7 +132,7 @@ void free_all(akua_pbf* s) {
                     s->sizeg, s->rhog, s->lamg, s->rrefg, s->mkey, s->r2i, s->blen, s->order, s->bmix,
                     s->ka0, s->va0, s->ka1, s->va1, s->kb0, s->vb0, s->kb1, s->vb1,
                     s->sort_scratch, s->table, s->nbr, s->cnt, s->flags, s->staging,
-                    s->feat, s->lacc, s->lprev, s->lacc_ref, s->vs4, s->err_max, s->err_sum};
+                    s->feat, s->lacc, s->lprev, s->lacc_ref, s->speed, s->err_max, s->err_sum};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (s->exec) cudaGraphExecDestroy(s->exec);
@@ -230,7 +230,7 @@ cudaError_t ensure_learn_buffers(akua_pbf* s) {
     if (e == cudaSuccess) e = dalloc(s, &s->lacc, n);
     if (e == cudaSuccess) e = dalloc(s, &s->lprev, n);
     if (e == cudaSuccess) e = dalloc(s, &s->lacc_ref, n);
-    if (e == cudaSuccess) e = dalloc(s, &s->vs4, n);
+    if (e == cudaSuccess) e = dalloc(s, &s->speed, n);
     if (e == cudaSuccess) e = dalloc(s, &s->err_max, 1);
     if (e == cudaSuccess) e = dalloc(s, &s->err_sum, 1);
     if (e == cudaSuccess) e = cudaMemset(s->lacc, 0, sizeof(float) * n);
@@ -265,13 +265,8 @@ void enqueue_pairs(akua_pbf* s, cudaStream_t st, Marker& mark) {
     akua::k_search<EXACT><<<grid_for(n, akua::kSearchBlock), akua::kSearchBlock,
                             akua::kSearchSmem, st>>>(
         s->d_params, s->ps0, s->xref, s->table, s->r2i, s->nbr, s->cnt, s->rho, s->lam,
-        s->flags, iters > 0 ? 1 : 0, learn ? s->vs4 : nullptr, learn ? s->lacc : nullptr);
+        s->flags, iters > 0 ? 1 : 0, s->speed, s->lprev, s->lacc, learn ? s->feat : nullptr);
     mark("k_search");
-    if (learn) {
-        akua::k_features<<<gp, akua::kPairBlock, 0, st>>>(s->d_params, s->ps0, s->vs4, s->lam,
-                                                           s->lprev, nbr4, s->cnt, s->feat);
-        mark("k_features");
-    }
     if (learn == 2) {
         akua::mlp::enqueue_forward(s->warm, s->feat, n, s->lam, s->lacc, st);
         mark("k_mlp_forward");
@@ -284,7 +279,8 @@ void enqueue_pairs(akua_pbf* s, cudaStream_t st, Marker& mark) {
         float4* nxt = ps[(it + 1) & 1];
         if (it > 0) {
             akua::k_density_lambda<EXACT><<<gp, akua::kPairBlock, 0, st>>>(
-                s->d_params, cur, nbr4, s->cnt, s->rho, s->lam, learn ? s->lacc : nullptr);
+                s->d_params, cur, nbr4, s->cnt, s->rho, s->lam,
+                learn == 1 ? s->lacc : nullptr);  // warm: the network's estimate is the sum
             mark("k_density_lambda");
         }
         if (it + 1 < iters) {
@@ -338,7 +334,7 @@ void enqueue_body(akua_pbf* s, cudaStream_t st, const char* aos, size_t stride, 
         s->d_params, s->spperm, s->refperm, s->x4, s->v4, s->col4, s->size, s->rref, s->x4g,
         s->col4g, s->sizeg, s->ps0, s->r2i, s->rrefg, s->xref, s->order, s->rho, s->lam, s->dp4,
         s->rhog, s->lamg, s->dpg, carry ? 1 : 0, s->lacc, s->lprev,
-        learn_mode(s) ? s->vs4 : nullptr);
+        learn_mode(s) ? s->speed : nullptr);
     mark("k_gather");
     akua::k_ref_table<<<ge, akua::kElemBlock, 0, st>>>(s->d_params, s->kr, s->table, s->bmix);
     mark("k_ref_table");

@@ -13,6 +13,7 @@ The reference reports no errors; every failing call here raises AkuaError.
 from __future__ import annotations
 
 import ctypes
+import dataclasses
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -85,8 +86,10 @@ class PBFSolver:
                  table_size: int | None = None, stream=None):
         self._lib = load_library()
         self.numParticles = int(numParticles)
-        self.config = config or PBFConfig()
-        self.corrParams = corrParams or LambdaCorrParams()
+        # own copies: setters below update them
+        self.config = dataclasses.replace(config) if config is not None else PBFConfig()
+        self.corrParams = (dataclasses.replace(corrParams) if corrParams is not None
+                           else LambdaCorrParams())
         self._cfg = self.config.to_c()
         self._corr = self.corrParams.to_c()
         h = ctypes.c_void_p()

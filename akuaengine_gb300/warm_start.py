@@ -51,9 +51,7 @@ class LambdaNet:
         h = ctypes.c_void_p()
         check(self._lib.akua_mlp_create(ctypes.byref(h)), "akua_mlp_create")
         self._h = h
-        self.norm = np.concatenate([np.zeros(8), np.ones(8), [1.0]]).astype(np.float32)
-        self.out_scale = 1.0  # lambda units of one network output unit, as trained
-        self.gain = 1.0       # multiplier applied when the prediction is used in a step
+        self.norm = np.concatenate([np.zeros(8), np.ones(8), [1.0, 1.0]]).astype(np.float32)
         self.set_params(init_params(seed) if params is None else params)
 
     @property
@@ -73,26 +71,29 @@ class LambdaNet:
               "akua_mlp_get_params")
         return p
 
-    def set_normalization(self, mean, inv_std, out_scale: float) -> None:
+    def set_normalization(self, mean, inv_std, out_scale: float, blend: float = 1.0) -> None:
         norm = np.concatenate([np.asarray(mean, np.float32).reshape(8),
                                np.asarray(inv_std, np.float32).reshape(8),
-                               [np.float32(out_scale)]]).astype(np.float32)
+                               [np.float32(out_scale), np.float32(blend)]]).astype(np.float32)
         check(self._lib.akua_mlp_set_normalization(self._h, norm.ctypes.data_as(ctypes.c_void_p),
                                                    MLP_NORM), "akua_mlp_set_normalization")
         self.norm = norm
-        self.out_scale = float(out_scale)
-        self.gain = 1.0
 
-    def set_gain(self, gain: float) -> None:
-        """Scales the prediction the step uses (the trained output scale times `gain`).  Set it
-        after training: the loss is defined on the scaled output."""
-        scale, mean, inv = self.out_scale, self.norm[:8].copy(), self.norm[8:16].copy()
-        self.set_normalization(mean, inv, scale * float(gain))
-        self.out_scale = scale
-        self.gain = float(gain)
+    @property
+    def out_scale(self) -> float:
+        return float(self.norm[16])
+
+    @property
+    def blend(self) -> float:
+        return float(self.norm[17])
+
+    def set_blend(self, blend: float) -> None:
+        """The lambda a step uses: lambda0 + blend * (estimate - lambda0)."""
+        self.set_normalization(self.norm[:8], self.norm[8:16], self.out_scale, float(blend))
 
     def fit_normalization(self, features, targets) -> None:
-        """Per-feature mean and 1/std, and the targets' standard deviation as output scale."""
+        """Per-feature mean and 1/std, and the targets' standard deviation as output scale
+        (blend 1)."""
         import torch
 
         f = features.double()
@@ -136,16 +137,14 @@ class LambdaNet:
         check(self._lib.akua_mlp_synchronize(self._h, _stream(stream)), "akua_mlp_synchronize")
 
     def save(self, path: str) -> None:
-        np.savez(path, params=self.params(), norm=self.norm, out_scale=self.out_scale,
-                 gain=self.gain)
+        np.savez(path, params=self.params(), norm=self.norm)
 
     @classmethod
     def load(cls, path: str) -> "LambdaNet":
         d = np.load(path)
         net = cls(params=d["params"])
         norm = d["norm"]
-        net.set_normalization(norm[:8], norm[8:16], float(d["out_scale"]))
-        net.set_gain(float(d["gain"]))
+        net.set_normalization(norm[:8], norm[8:16], float(norm[16]), float(norm[17]))
         return net
 
     def close(self) -> None:
@@ -252,17 +251,20 @@ def rollout_errors(sc, cfg, corr, iterations: int, net=None, steps: int = 60, st
     return np.array(errs)
 
 
-def calibrate_gain(net: LambdaNet, sc, cfg, corr, iterations: int,
-                   gains=(0.3, 0.4, 0.5, 0.6, 0.75), steps: int = 60, stream=None) -> dict:
-    """Picks the gain whose rollout of `sc` has the lowest mean |C| (max C breaks ties) and sets
-    it; returns {gain: (mean of max C, mean of mean |C|)}."""
+def calibrate_blend(net: LambdaNet, sc, cfg, corr, iterations: int,
+                    blends=(0.0, 0.05, 0.1, 0.15, 0.2, 0.3, 0.4, 0.5), steps: int = 60,
+                    stream=None) -> dict:
+    """Picks the blend whose rollout of `sc` has the lowest per-step max density error averaged
+    over the rollout (mean |C| breaks ties) and sets it; blend 0 is the plain solver, so the
+    choice is never worse than plain on that rollout.  Returns {blend: (mean of max C, mean of
+    mean |C|)}."""
     res = {}
-    for g in gains:
-        net.set_gain(g)
+    for g in blends:
+        net.set_blend(g)
         e = rollout_errors(sc, cfg, corr, iterations, net, steps, stream)
         bad = not np.isfinite(e).all()
         res[float(g)] = (float("inf"), float("inf")) if bad else (float(e[:, 0].mean()),
                                                                   float(e[:, 1].mean()))
-    best = min(res, key=lambda g: (res[g][1], res[g][0]))
-    net.set_gain(best)
+    best = min(res, key=lambda g: (res[g][0], res[g][1]))
+    net.set_blend(best)
     return res

@@ -80,6 +80,9 @@ def parse_args(argv=None):
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--exact", action="store_true", help="IEEE math in pair terms")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="skip the learned warm-start comparison")
+    ap.add_argument("--learned-iterations", type=int, default=2)
     return ap.parse_args(argv)
 
 
@@ -205,6 +208,99 @@ def run_reference(args, sc, cfg, corr):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------------- learned
+def run_learned(args, sc, cfg, corr, stream, plain_value, plain_ms):
+    """Learned warm start against the plain 4-iteration step on the same workload: trains the
+    network on pairs from a 20-iteration teacher run of a differently seeded copy of the scene
+    (4 captures of every particle), calibrates its blend on that copy, then times the
+    warm-started step with fewer iterations and measures both solvers' density-constraint error
+    over rollouts of the benchmark scene."""
+    import numpy as np
+    import torch
+
+    from akuaengine_gb300 import PBFSolver, scene
+    from akuaengine_gb300.warm_start import (LambdaNet, calibrate_blend, collect_pairs,
+                                             rollout_errors, train)
+
+    t0 = time.perf_counter()
+    train_sc = scene.workload(args.workload, seed=1)
+    x, y = collect_pairs(train_sc, cfg, corr, steps=123, capture_every=40, first_capture=2,
+                         stream=stream)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    net = LambdaNet(seed=0)
+    net.fit_normalization(x, y)
+    losses = train(net, x, y, epochs=6, batch=65536, stream=stream)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    it = args.learned_iterations
+    steps = 60
+    cal = calibrate_blend(net, train_sc, cfg, corr, iterations=it, steps=steps, stream=stream)
+    t3 = time.perf_counter()
+    del x, y
+
+    # timing: the warm-started step, device-timed like the main line
+    solver = PBFSolver(sc.n, cfg, corr, stream=stream)
+    solver.set_solver_iterations(it)
+    solver.set_warm_start(net)
+    buf = torch.from_numpy(sc.particles.view(np.uint8).copy()).cuda()
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            solver.step(buf, sc.dt, sc.box_min, sc.box_max)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        solver.step(buf, sc.dt, sc.box_min, sc.box_max)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    launches = solver.kernels_per_step()
+    solver.profile_begin(3)
+    for _ in range(3):
+        solver.step(buf, sc.dt, sc.box_min, sc.box_max)
+    prof = solver.profile_end()
+    solver.close()
+
+    # accuracy: rollouts from the benchmark scene's initial state
+    e_plain = rollout_errors(sc, cfg, corr, cfg.solverIterations, None, steps, stream)
+    e_warm = rollout_errors(sc, cfg, corr, it, net, steps, stream)
+    e_plain_same = rollout_errors(sc, cfg, corr, it, None, steps, stream)
+    net.close()
+    value = args.steps / (ms / 1000.0)
+    return {
+        "method": "iteration 1 uses lambda0 + blend * (network estimate - lambda0), then plain "
+                  "Jacobi iterations; blend calibrated on the training scene (0 = plain)",
+        "warm_iterations": it, "plain_iterations": cfg.solverIterations,
+        "steps_per_s": round(value, 2), "ms_per_step": round(ms / args.steps, 4),
+        "speedup_vs_plain": round(value / plain_value, 4),
+        "gpu_launches_per_step": launches,
+        "density_error": {
+            "rollout_steps": steps,
+            "warm": {"max": round(float(e_warm[:, 0].mean()), 5),
+                     "worst": round(float(e_warm[:, 0].max()), 5),
+                     "mean_abs": round(float(e_warm[:, 1].mean()), 5)},
+            "plain": {"max": round(float(e_plain[:, 0].mean()), 5),
+                      "worst": round(float(e_plain[:, 0].max()), 5),
+                      "mean_abs": round(float(e_plain[:, 1].mean()), 5)},
+            "plain_same_iterations": {"max": round(float(e_plain_same[:, 0].mean()), 5),
+                                      "mean_abs": round(float(e_plain_same[:, 1].mean()), 5)},
+            "definition": "per step: max_i max(rho_i/rho0 - 1, 0) and mean_i |rho_i/rho0 - 1| at "
+                          "the step's final positions over its lists; averaged over the rollout",
+        },
+        "training": {"pairs": int(4 * sc.n), "teacher_iterations": 20, "epochs": 6,
+                     "batch": 65536, "final_loss": round(losses[-1], 5),
+                     "collect_s": round(t1 - t0, 2), "train_s": round(t2 - t1, 2),
+                     "calibrate_s": round(t3 - t2, 2), "blend": net.blend,
+                     "blend_sweep": {str(k): [round(v[0], 5), round(v[1], 5)]
+                                     for k, v in cal.items()},
+                     "data": "seed-1 copy of the workload (evaluation uses seed 0)"},
+        "kernels_us": {k: round(1000.0 * v[1] / max(v[0], 1), 2) for k, v in prof.items()
+                       if k in ("k_features", "k_mlp_forward", "k_search", "k_delta_correct",
+                                "k_density_lambda", "k_delta_final")},
+    }
+
+
 # ---------------------------------------------------------------------------------- GPU arm
 def run_ours(args, sc, cfg, corr):
     import numpy as np
@@ -315,6 +411,10 @@ def run_ours(args, sc, cfg, corr):
                "h2d_bytes_per_step": int(host.nbytes), "d2h_bytes_per_step": int(host.nbytes),
                "api": "akua_pbf_step_host (pinned host records)"}
 
+    learned = None
+    if not args.no_learned and cfg.solverIterations > args.learned_iterations:
+        learned = run_learned(args, sc, cfg, corr, stream, value / world, ms / args.steps)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         sps, psps, cores, sample = time_oracle(sc, cfg, corr, 3, 30.0)
@@ -344,6 +444,7 @@ def run_ours(args, sc, cfg, corr):
             "gpu_launches": launches_per_step * args.steps,
             "clocks": clocks,
             "kernels": kernels,
+            "learned_warm_start": learned,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

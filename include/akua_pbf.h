@@ -197,11 +197,15 @@ int akua_sort_pairs_noalloc(const uint32_t* keysIn, const uint32_t* valsIn, uint
  * of the neighbours, the SPH divergence of the predicted velocity, |predicted velocity|.
  * Parameters (float[AKUA_MLP_PARAMS], FP32 master copy): W1[64][8], b1[64], W2[64][64], b2[64],
  * W3[64][64], b3[64], w4[64], b4.  Normalisation (float[AKUA_MLP_NORM]): mean[8], inv_std[8] of
- * the features, and the output scale (the network's output times it is lambda). */
+ * the features, the output scale (the network's output times it is the estimate p of the
+ * accumulated lambda) and the blend b: the lambda used (by a step, and by akua_mlp_forward) is
+ * lambda0 + b (p - lambda0) with lambda0 = feature 3 (b = 1 gives p; b = 0 the plain solver's
+ * lambda).  In a warm-started step, p itself is what the next step sees as the previous step's
+ * accumulated lambda. */
 #define AKUA_MLP_INPUTS 8
 #define AKUA_MLP_HIDDEN 64
 #define AKUA_MLP_PARAMS 8961
-#define AKUA_MLP_NORM 17
+#define AKUA_MLP_NORM 18
 typedef struct akua_mlp akua_mlp;
 /* Allocates the network on the current device (zero parameters, identity normalisation). */
 int akua_mlp_create(akua_mlp** out);

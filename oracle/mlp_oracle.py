@@ -8,7 +8,8 @@ weights W1..W3) and computes everything else in float64; with `emulate=False` it
 float64 network, whose analytic gradient is checked against finite differences.
 
 Parameter layout (flat float32[8961]): W1[64][8], b1[64], W2[64][64], b2[64], W3[64][64], b3[64],
-w4[64], b4.  Normalisation (float32[17]): mean[8], inv_std[8], output scale.
+w4[64], b4.  Normalisation (float32[18]): mean[8], inv_std[8], output scale, blend (the blend
+only mixes the output with an input feature when a step uses it; `forward` returns the estimate).
 """
 from __future__ import annotations
 
@@ -18,7 +19,7 @@ N_IN, N_HID = 8, 64
 SIZES = [("W1", (N_HID, N_IN)), ("b1", (N_HID,)), ("W2", (N_HID, N_HID)), ("b2", (N_HID,)),
          ("W3", (N_HID, N_HID)), ("b3", (N_HID,)), ("w4", (N_HID,)), ("b4", (1,))]
 N_PARAMS = sum(int(np.prod(s)) for _, s in SIZES)
-N_NORM = 2 * N_IN + 1
+N_NORM = 2 * N_IN + 2
 
 
 def bf16(x) -> np.ndarray:

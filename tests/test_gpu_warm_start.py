@@ -54,7 +54,7 @@ def test_capture_invariants(cuda_lib):
 
 @pytest.fixture(scope="module")
 def trained(cuda_lib):
-    from akuaengine_gb300.warm_start import LambdaNet, calibrate_gain, collect_pairs, train
+    from akuaengine_gb300.warm_start import LambdaNet, calibrate_blend, collect_pairs, train
 
     sc = scene.workload("dam_break_27k", seed=0)
     cfg, corr = scene.benchmark_params()
@@ -63,7 +63,7 @@ def trained(cuda_lib):
     net.fit_normalization(x, y)
     _, loss0 = net.gradient(x, y)
     losses = train(net, x, y, epochs=25, batch=16384)
-    cal = calibrate_gain(net, sc, cfg, corr, iterations=2, steps=60)
+    cal = calibrate_blend(net, sc, cfg, corr, iterations=2, steps=90)
     yield net, loss0, losses, int(x.shape[0]), cal
     net.close()
 
@@ -71,7 +71,7 @@ def trained(cuda_lib):
 def test_training_reduces_loss(trained):
     net, loss0, losses, pairs, cal = trained
     print("pairs %d, loss %.4g -> %s" % (pairs, loss0, ["%.4g" % v for v in losses]))
-    print("gain calibration (iterations 2): %s -> %.2f" % (cal, net.gain))
+    print("blend calibration (iterations 2): %s -> %.2f" % (cal, net.blend))
     assert losses[-1] < 0.1 * loss0
 
 
@@ -91,11 +91,11 @@ def test_warm_start_gains_over_plain_solver(trained):
         res[name] = e
         print("%-7s max C %.5f (worst %.5f)  mean |C| %.5f"
               % (name, e[:, 0].mean(), e[:, 0].max(), e[:, 1].mean()))
-    assert res["warm2"][:, 1].mean() < res["plain2"][:, 1].mean()
     assert res["warm2"][:, 0].mean() < res["plain2"][:, 0].mean()
+    assert res["warm2"][:, 1].mean() < res["plain2"][:, 1].mean()
 
 
-def test_warm_start_launches_features_and_network(trained):
+def test_warm_start_launches_the_network(trained):
     net = trained[0]
     sc = scene.workload("dam_break_27k", seed=2)
     counts = []
@@ -104,4 +104,4 @@ def test_warm_start_launches_features_and_network(trained):
         s.step(buf, sc.dt, sc.box_min, sc.box_max)
         counts.append(s.kernels_per_step())
         s.close()
-    assert counts[1] == counts[0] + 2
+    assert counts[1] == counts[0] + 1  # the network's forward pass; features come from the walk

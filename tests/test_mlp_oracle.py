@@ -12,14 +12,14 @@ def _problem(seed=0, n=64):
         rng.normal(0, 1 / np.sqrt(64), 64 * 64), rng.normal(0, 0.1, 64),
         rng.normal(0, 1 / np.sqrt(64), 64 * 64), rng.normal(0, 0.1, 64),
         rng.normal(0, 1 / np.sqrt(64), 64), rng.normal(0, 0.1, 1)])
-    norm = np.concatenate([rng.normal(0, 1, 8), rng.uniform(0.5, 2, 8), [1.7]])
+    norm = np.concatenate([rng.normal(0, 1, 8), rng.uniform(0.5, 2, 8), [1.7, 1.0]])
     feat = rng.normal(0, 1.5, (n, 8))
     target = rng.normal(0, 1, n)
     return params, norm, feat, target
 
 
 def test_param_count():
-    assert mo.N_PARAMS == 8961 and mo.N_NORM == 17
+    assert mo.N_PARAMS == 8961 and mo.N_NORM == 18
 
 
 def test_gradient_matches_finite_differences():
