@@ -11,8 +11,9 @@ from ._abi import (  # noqa: F401
     OPT_EXACT_MATH, OPT_NO_GRAPH, OPT_RESIDENT, PARTICLE_DTYPE, AkuaError, exported_symbols,
     load_library,
 )
-from .scene import Scene, benchmark_params, dam_break, double_dam_break, reference_dam_break, workload  # noqa: F401
-from .solver import LambdaCorrParams, ParticleBuffer, PBFConfig, PBFSolver  # noqa: F401
+from .scene import (Scene, SceneBatch, batched_dam_breaks, benchmark_params, dam_break,  # noqa: F401
+                    double_dam_break, reference_dam_break, workload)
+from .solver import BatchSolver, LambdaCorrParams, ParticleBuffer, PBFConfig, PBFSolver  # noqa: F401
 
 __all__ = [
     "PBFSolver", "PBFConfig", "LambdaCorrParams", "ParticleBuffer", "PARTICLE_DTYPE", "AkuaError",

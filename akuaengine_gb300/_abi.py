@@ -65,6 +65,11 @@ class CCorr(ctypes.Structure):
     ]
 
 
+class CSceneDesc(ctypes.Structure):
+    _fields_ = [("numParticles", ctypes.c_int32), ("gravity", ctypes.c_float * 3),
+                ("boxMin", ctypes.c_float * 3), ("boxMax", ctypes.c_float * 3)]
+
+
 class CStats(ctypes.Structure):
     _fields_ = [
         ("numParticles", ctypes.c_int32),
@@ -128,6 +133,11 @@ _SIGS = {
                                             ctypes.POINTER(ctypes.c_int32)]),
     "akua_sort_pairs_noalloc": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int32, ctypes.c_int32, _P]),
     "akua_pbf_set_solver_iterations": (ctypes.c_int, [_P, ctypes.c_int32]),
+    "akua_pbf_create_batch": (ctypes.c_int, [ctypes.c_int32, ctypes.POINTER(CSceneDesc),
+                                             ctypes.POINTER(CConfig), ctypes.POINTER(CCorr),
+                                             ctypes.POINTER(_P)]),
+    "akua_pbf_step_batch": (ctypes.c_int, [_P, ctypes.c_float]),
+    "akua_pbf_set_scene": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.POINTER(CSceneDesc)]),
     "akua_mlp_create": (ctypes.c_int, [ctypes.POINTER(_P)]),
     "akua_mlp_destroy": (ctypes.c_int, [_P]),
     "akua_mlp_set_params": (ctypes.c_int, [_P, _P, ctypes.c_int32]),

@@ -49,7 +49,20 @@ struct StepParams {
     // Morton key of the walk cell: cell - sp_origin per axis, clamped to sp_bits bits
     int32_t sp_origin[3];
     int32_t sp_bits;
+    // Batches of independent scenes: this scene's index, its first bucket in the shared table
+    // (hash keys are table_offset + hash, so one sort orders by (scene, hash)), and the scene of
+    // every particle (null for a single scene).  Scenes occupy the same index range in every
+    // particle order (import, reference, internal), so one array serves all kernels.
+    int32_t scene;
+    uint32_t table_offset;
+    const uint16_t* scene_of;
 };
+
+// The parameters of the scene particle (or reference rank, or internal slot) i belongs to.
+__device__ __forceinline__ const StepParams& params_for(const StepParams* P, int i) {
+    const uint16_t* sid = P->scene_of;
+    return sid ? P[sid[i]] : *P;
+}
 
 __device__ __forceinline__ float fmaf_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 

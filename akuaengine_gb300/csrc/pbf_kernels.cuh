@@ -55,6 +55,17 @@ __global__ void k_set_params(StepParams p, StepParams* __restrict__ dst) {
     if (threadIdx.x == 0 && blockIdx.x == 0) *dst = p;
 }
 
+// Per-scene parameters of a batch, uploaded in chunks passed by value (kernel parameters are
+// captured at launch, so the host copy may change right after).
+constexpr int kParamChunk = 16;  // 16 x 168 bytes: under the classic 4 KB parameter limit
+struct ParamChunk {
+    StepParams p[kParamChunk];
+    int count;
+};
+__global__ void k_set_params_chunk(ParamChunk c, StepParams* __restrict__ dst) {
+    if (blockIdx.x == 0 && threadIdx.x < c.count) dst[threadIdx.x] = c.p[threadIdx.x];
+}
+
 // Reads the attached records (buffer order = previous reference order) into the state.  A block
 // stages its records through shared memory so global reads are coalesced when records are packed.
 // With `carry`, density, lambda and position_delta are read too: with zero solver iterations the
@@ -126,16 +137,17 @@ __global__ void __launch_bounds__(kElemBlock)
     k_keys(const StepParams* __restrict__ P, const float4* __restrict__ x4,
            const float4* __restrict__ v4, const uint32_t* __restrict__ rref,
            uint32_t* __restrict__ akey, uint32_t* __restrict__ aval, uint32_t* __restrict__ mkey) {
-    const StepParams& p = *P;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n) return;
+    if (i >= P->n) return;
+    const StepParams& p = params_for(P, i);
     const float3 xs = predict(p, x4[i], v4[i]);
     const uint32_t h = cell_hash(cell_coord(xs.x, p.hash_cell), cell_coord(xs.y, p.hash_cell),
                                  cell_coord(xs.z, p.hash_cell), p.table_size, p.table_magic);
     const uint32_t r = rref[i];
-    akey[r] = h;
+    akey[r] = p.table_offset + h;
     aval[r] = (uint32_t)i;
-    mkey[i] = morton_key(p, cell_coord(xs.x, p.search_cell), cell_coord(xs.y, p.search_cell),
+    mkey[i] = ((uint32_t)p.scene << (3 * p.sp_bits)) |
+              morton_key(p, cell_coord(xs.x, p.search_cell), cell_coord(xs.y, p.search_cell),
                          cell_coord(xs.z, p.search_cell));
 }
 
@@ -166,9 +178,9 @@ __global__ void __launch_bounds__(kElemBlock)
              float* __restrict__ lam_out, float4* __restrict__ dp_out, int carry,
              const float* __restrict__ lacc_src, float* __restrict__ lprev_out,
              float* __restrict__ speed_out) {
-    const StepParams& p = *P;
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= p.n) return;
+    if (s >= P->n) return;
+    const StepParams& p = params_for(P, s);
     const uint32_t r = spr[s];
     const uint32_t o = refperm[r];
     const float4 x = x4[o];
@@ -262,7 +274,8 @@ __global__ void __launch_bounds__(kElemBlock)
 // holds the particle of reference rank r), staged through shared memory so global writes are
 // coalesced when records are packed.
 __global__ void __launch_bounds__(kIoBlock)
-    k_export(char* __restrict__ aos, uint64_t stride, int n, const uint32_t* __restrict__ r2i,
+    k_export(const StepParams* __restrict__ P, char* __restrict__ aos, uint64_t stride, int n,
+             const uint32_t* __restrict__ r2i,
              const uint32_t* __restrict__ kr, const float4* __restrict__ x4,
              const float4* __restrict__ v4, const float4* __restrict__ vstar4,
              const float4* __restrict__ dp4, const float4* __restrict__ om4,
@@ -288,7 +301,7 @@ __global__ void __launch_bounds__(kIoBlock)
         o[kMass] = x.w;
         o[kDensity] = rho[s];
         o[kLambda] = lam[s];
-        o[kHash] = __uint_as_float(kr[r]);
+        o[kHash] = __uint_as_float(kr[r] - params_for(P, r).table_offset);  // the scene's own hash
         o[kColor] = c.x; o[kColor + 1] = c.y; o[kColor + 2] = c.z; o[kColor + 3] = c.w;
         o[kSize] = size[s];
     }

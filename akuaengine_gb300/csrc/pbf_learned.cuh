@@ -4,8 +4,9 @@
 // The warm start replaces iteration 1's lambda (the one-step Jacobi estimate) by the network's
 // prediction of the lambda a 20-iteration solve accumulates over the step (the sum of its
 // iterations' lambdas, which is what drives the total position correction since delta-p is linear
-// in lambda), scaled by a calibrated gain.  Later iterations run the reference's update unchanged,
-// so the plain iterated solver still corrects whatever the prediction leaves.
+// in lambda), blended with iteration 1's lambda by a calibrated factor.  Later iterations run the
+// reference's update unchanged, so the plain iterated solver still corrects whatever the
+// prediction leaves.
 //
 // Features of particle i at the start of the step, all by-products of iteration 1's density and
 // lambda over the step's neighbour list (the walk writes them; no extra neighbour pass):
@@ -50,11 +51,11 @@ __global__ void __launch_bounds__(128)
     k_density_error(const StepParams* __restrict__ P, const float4* __restrict__ x4,
                     const uint4* __restrict__ nbr4, const uint32_t* __restrict__ cnt,
                     uint32_t* __restrict__ max_bits, double* __restrict__ sum_abs) {
-    const StepParams& p = *P;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int n = p.n;
+    const int n = P->n;
     float e = 0.f, m = 0.f;
     if (i < n) {
+        const StepParams& p = params_for(P, i);
         const float4 xi = x4[i];
         float rho = xi.w * p.w0;
         const int c = (int)cnt[i];

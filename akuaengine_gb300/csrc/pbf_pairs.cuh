@@ -125,8 +125,9 @@ __global__ void __launch_bounds__(128)
                      const uint4* __restrict__ nbr4, const uint32_t* __restrict__ cnt,
                      float* __restrict__ rho_out, float* __restrict__ lam_out,
                      float* __restrict__ lacc) {
-    const StepParams& p = *P;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P->n) return;
+    const StepParams& p = params_for(P, i);
     const int n = p.n;
     if (i >= n) return;
     const float4 xi = ps[i];
@@ -208,8 +209,9 @@ __global__ void __launch_bounds__(128)
                     const float* __restrict__ lam, const uint4* __restrict__ nbr4,
                     const uint32_t* __restrict__ cnt, float4* __restrict__ ps_out,
                     float4* __restrict__ dp4) {
-    const StepParams& p = *P;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P->n) return;
+    const StepParams& p = params_for(P, i);
     if (i >= p.n) return;
     const float4 xi = ps_in[i];
     const float3 d = position_delta<EXACT>(p, p.n, xi, lam[i], ps_in, lam, nbr4 + i, (int)cnt[i]);
@@ -257,8 +259,9 @@ __global__ void __launch_bounds__(128)
                   uint32_t* __restrict__ rref, const float* __restrict__ rho_c,
                   const float* __restrict__ lam_c, const float4* __restrict__ dp_c,
                   float* __restrict__ rho, float* __restrict__ lam_out, int has_delta) {
-    const StepParams& p = *P;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P->n) return;
+    const StepParams& p = params_for(P, i);
     if (i >= p.n) return;
     const float4 xi = ps_in[i];
     float nx = xi.x, ny = xi.y, nz = xi.z;
@@ -300,8 +303,9 @@ __global__ void __launch_bounds__(128)
     k_vorticity(const StepParams* __restrict__ P, const float4* __restrict__ x4,
                 const float4* __restrict__ v4, const uint4* __restrict__ nbr4,
                 const uint32_t* __restrict__ cnt, float4* __restrict__ om4) {
-    const StepParams& p = *P;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P->n) return;
+    const StepParams& p = params_for(P, i);
     const int n = p.n;
     if (i >= n) return;
     const float4 xi = x4[i], vi = v4[i];
@@ -341,8 +345,9 @@ __global__ void __launch_bounds__(128)
               const float4* __restrict__ v4, const float4* __restrict__ om4,
               const float* __restrict__ rho, const uint4* __restrict__ nbr4,
               const uint32_t* __restrict__ cnt, float4* __restrict__ vc4) {
-    const StepParams& p = *P;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P->n) return;
+    const StepParams& p = params_for(P, i);
     const int n = p.n;
     if (i >= n) return;
     const float4 xi = x4[i], vi = v4[i], wi = om4[i];
@@ -393,8 +398,9 @@ __global__ void __launch_bounds__(128)
     k_xsph(const StepParams* __restrict__ P, const float4* __restrict__ x4,
            const float4* __restrict__ vc4, const uint4* __restrict__ nbr4,
            const uint32_t* __restrict__ cnt, float4* __restrict__ v4) {
-    const StepParams& p = *P;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P->n) return;
+    const StepParams& p = params_for(P, i);
     const int n = p.n;
     if (i >= n) return;
     const float4 xi = x4[i], vi = vc4[i];

@@ -70,11 +70,14 @@ __global__ void __launch_bounds__(kSearchBlock)
     const int cx = cell_coord(xi.x, p.search_cell);
     const int cy = cell_coord(xi.y, p.search_cell);
     const int cz = cell_coord(xi.z, p.search_cell);
+    // a run: consecutive particles of one scene in one cell
+    const int sid = (valid && p.scene_of) ? (int)p.scene_of[i] : 0;
     const int px = __shfl_up_sync(kFullWarp, cx, 1);
     const int py = __shfl_up_sync(kFullWarp, cy, 1);
     const int pz = __shfl_up_sync(kFullWarp, cz, 1);
-    uint32_t starts =
-        __ballot_sync(kFullWarp, valid && (lane == 0 || px != cx || py != cy || pz != cz));
+    const int ps_ = __shfl_up_sync(kFullWarp, sid, 1);
+    uint32_t starts = __ballot_sync(
+        kFullWarp, valid && (lane == 0 || px != cx || py != cy || pz != cz || ps_ != sid));
     const int nvalid = min(32, n - base);
     __syncwarp();
 
@@ -89,11 +92,13 @@ __global__ void __launch_bounds__(kSearchBlock)
         const int rx = __shfl_sync(kFullWarp, cx, q0);
         const int ry = __shfl_sync(kFullWarp, cy, q0);
         const int rz = __shfl_sync(kFullWarp, cz, q0);
+        const StepParams& pr = P[__shfl_sync(kFullWarp, sid, q0)];  // the run's scene
         // lane b < 27 holds bucket b of the walk (dx = b/9 - 1, dy = b/3%3 - 1, dz = b%3 - 1)
         uint2 e = make_uint2(0u, 0u);
         if (lane < 27)
-            e = __ldg(table + cell_hash(rx + lane / 9 - 1, ry + lane / 3 % 3 - 1,
-                                        rz + lane % 3 - 1, p.table_size, p.table_magic));
+            e = __ldg(table + pr.table_offset +
+                      cell_hash(rx + lane / 9 - 1, ry + lane / 3 % 3 - 1, rz + lane % 3 - 1,
+                                pr.table_size, pr.table_magic));
         const uint32_t blen = e.y & ~kMixedBucket;
         uint32_t incl = blen;
 #pragma unroll
@@ -172,7 +177,8 @@ __global__ void __launch_bounds__(kSearchBlock)
         lam_out[i] = l;
         if (feat) {  // learned modes: the lambda sum starts; the network's features
             lacc[i] = l;
-            write_features(p, acc, l, count, lprev[i], speed[i], feat + (size_t)kFeatures * i);
+            write_features(params_for(P, i), acc, l, count, lprev[i], speed[i],
+                           feat + (size_t)kFeatures * i);
         }
     }
 }

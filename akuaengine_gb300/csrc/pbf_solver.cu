@@ -94,6 +94,12 @@ struct akua_pbf {
     double* err_sum = nullptr;
     int graph_learn = 0;
 
+    // batches of independent scenes (akua_pbf_create_batch); empty for a single scene
+    std::vector<akua_scene_desc> scenes;
+    std::vector<uint32_t> scene_first;  // first particle of each scene
+    uint16_t* scene_of = nullptr;       // device: the scene of every particle
+    int scene_bits = 0;                 // bits of the scene index in the Morton sort key
+
     int64_t steps = 0;
     uint64_t device_bytes = 0;
 
@@ -132,7 +138,8 @@ void free_all(akua_pbf* s) {
                     s->sizeg, s->rhog, s->lamg, s->rrefg, s->mkey, s->r2i, s->blen, s->order, s->bmix,
                     s->ka0, s->va0, s->ka1, s->va1, s->kb0, s->vb0, s->kb1, s->vb1,
                     s->sort_scratch, s->table, s->nbr, s->cnt, s->flags, s->staging,
-                    s->feat, s->lacc, s->lprev, s->lacc_ref, s->speed, s->err_max, s->err_sum};
+                    s->feat, s->lacc, s->lprev, s->lacc_ref, s->speed, s->err_max, s->err_sum,
+                    s->scene_of};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (s->exec) cudaGraphExecDestroy(s->exec);
@@ -168,6 +175,7 @@ int morton_bits(const akua_pbf* s, const float* bmin, const float* bmax, int ori
     while (bits < 10 && (double)(1 << bits) < extent) ++bits;
     return bits;
 }
+
 
 // Kernel constants, evaluated on the host in the order the device and the host restatement use.
 // Host code is compiled with -ffp-contract=off.
@@ -215,6 +223,37 @@ StepParams make_params(const akua_pbf* s, float dt, const float* bmin, const flo
     p.table_magic = UINT64_MAX / (uint64_t)s->table_size + 1u;
     p.sp_bits = morton_bits(s, bmin, bmax, p.sp_origin);
     return p;
+}
+
+// Parameters of every scene of a batch for one step.  The Morton keys of all scenes share one
+// bit count per axis (the largest any box needs, limited so that the scene index fits above
+// them in 32 bits; cells beyond it are clamped, which only costs locality).
+std::vector<StepParams> make_batch_params(const akua_pbf* s, float dt) {
+    const int ns = (int)s->scenes.size();
+    std::vector<StepParams> out(ns);
+    int bits = 1;
+    std::vector<int> origin(3 * ns);
+    for (int k = 0; k < ns; ++k)
+        bits = std::max(bits, morton_bits(s, s->scenes[k].boxMin, s->scenes[k].boxMax,
+                                          &origin[3 * k]));
+    bits = std::min(bits, (32 - s->scene_bits) / 3);
+    for (int k = 0; k < ns; ++k) {
+        const akua_scene_desc& d = s->scenes[k];
+        StepParams p = make_params(s, dt, d.boxMin, d.boxMax);
+        for (int a = 0; a < 3; ++a) {
+            p.gravity[a] = d.gravity[a];
+            p.sp_origin[a] = origin[3 * k + a];
+        }
+        p.sp_bits = bits;
+        // PBFSolver.cpp:15 per scene: maxNeighbours * N_s buckets, after the earlier scenes'
+        p.table_size = (uint32_t)(s->cfg.maxNeighbours * d.numParticles);
+        p.table_magic = UINT64_MAX / (uint64_t)p.table_size + 1u;
+        p.table_offset = (uint32_t)s->cfg.maxNeighbours * s->scene_first[k];
+        p.scene = k;
+        p.scene_of = s->scene_of;
+        out[k] = p;
+    }
+    return out;
 }
 
 inline int grid_for(int n, int block) { return (n + block - 1) / block; }
@@ -348,7 +387,7 @@ void enqueue_body(akua_pbf* s, cudaStream_t st, const char* aos, size_t stride, 
     else enqueue_pairs<false>(s, st, mark);
     if (aos) {
         akua::k_export<<<grid_for(n, akua::kIoBlock), akua::kIoBlock, 0, st>>>(
-            const_cast<char*>(aos), stride, n, s->r2i, s->kr, s->x4, s->v4, s->vstar4, s->dp4,
+            s->d_params, const_cast<char*>(aos), stride, n, s->r2i, s->kr, s->x4, s->v4, s->vstar4, s->dp4,
             s->om4, s->rho, s->lam, s->col4, s->size, s->lacc,
             learn_mode(s) ? s->lacc_ref : nullptr);
         mark("k_export");
@@ -367,7 +406,7 @@ void invalidate_graph(akua_pbf* s) {
 void update_plans(akua_pbf* s, int sp_bits) {
     s->plan_ref = akua::radix::make_plan(akua::radix::bits_for(s->table_size));
     s->sp_bits = sp_bits;
-    s->plan_sp = akua::radix::make_plan(3 * sp_bits);
+    s->plan_sp = akua::radix::make_plan(3 * sp_bits + s->scene_bits);
 }
 
 int ensure_graph(akua_pbf* s, const char* aos, size_t stride) {
@@ -401,10 +440,13 @@ int ensure_graph(akua_pbf* s, const char* aos, size_t stride) {
 
 int do_step(akua_pbf* s, const char* aos, size_t stride, bool force_import, float dt,
             const float* bmin, const float* bmax) {
-    if (!(std::isfinite(dt) && dt > 0.0f) || !finite3(bmin) || !finite3(bmax))
+    const bool batch = !s->scenes.empty();
+    if (!(std::isfinite(dt) && dt > 0.0f) || (!batch && (!finite3(bmin) || !finite3(bmax))))
         return AKUA_ERR_INVALID_ARGUMENT;
     cudaGetLastError();  // clear a stale error of an unrelated call
-    const StepParams p = make_params(s, dt, bmin, bmax);
+    const std::vector<StepParams> ps =
+        batch ? make_batch_params(s, dt) : std::vector<StepParams>{make_params(s, dt, bmin, bmax)};
+    const StepParams& p = ps[0];
     if (p.sp_bits != s->sp_bits) update_plans(s, p.sp_bits);
     cudaStream_t st = s->stream;
     const bool prof = s->prof_active && s->prof_steps_left > 0;
@@ -416,7 +458,16 @@ int do_step(akua_pbf* s, const char* aos, size_t stride, bool force_import, floa
             s->prof_names[s->prof_next++] = nullptr;
         }
     }
-    akua::k_set_params<<<1, 32, 0, st>>>(p, s->d_params);
+    if (!batch) {
+        akua::k_set_params<<<1, 32, 0, st>>>(p, s->d_params);
+    } else {
+        for (size_t k0 = 0; k0 < ps.size(); k0 += akua::kParamChunk) {
+            akua::ParamChunk c;
+            c.count = (int)std::min(ps.size() - k0, (size_t)akua::kParamChunk);
+            for (int k = 0; k < c.count; ++k) c.p[k] = ps[k0 + k];
+            akua::k_set_params_chunk<<<1, akua::kParamChunk, 0, st>>>(c, s->d_params + k0);
+        }
+    }
     mark("k_set_params");
     const bool import = force_import || !(s->options & AKUA_PBF_OPT_RESIDENT) || !s->state_valid;
     if (import) {
@@ -485,8 +536,14 @@ void akua_pbf_default_config(akua_pbf_config* c, akua_lambda_corr_params* k) {
     }
 }
 
-int akua_pbf_create(int32_t n, const akua_pbf_config* cfg, const akua_lambda_corr_params* corr,
-                    akua_pbf** out) {
+}  // extern "C"
+
+namespace {
+
+// A solver for one scene (scenes == nullptr) or for a batch of independent scenes laid out one
+// after another in the particle array.
+int create_solver(int32_t n, const akua_pbf_config* cfg, const akua_lambda_corr_params* corr,
+                  const akua_scene_desc* scenes, int32_t num_scenes, akua_pbf** out) {
     if (!out) return AKUA_ERR_INVALID_ARGUMENT;
     *out = nullptr;
     if (!cfg || !corr || n <= 0) return AKUA_ERR_INVALID_ARGUMENT;
@@ -494,23 +551,42 @@ int akua_pbf_create(int32_t n, const akua_pbf_config* cfg, const akua_lambda_cor
     if (!(cfg->smoothRadius > 0.0f) || !(cfg->spatialHashCellSize > 0.0f) ||
         !(cfg->restDensity > 0.0f) || !std::isfinite(cfg->smoothRadius))
         return AKUA_ERR_INVALID_ARGUMENT;
-    // PBFSolver.cpp:15: _tableSize = maxNeighbours * numParticles, an int.
-    if ((int64_t)cfg->maxNeighbours * (int64_t)n > (int64_t)INT_MAX) return AKUA_ERR_TOO_LARGE;
+    // PBFSolver.cpp:15: _tableSize = maxNeighbours * numParticles, an int (per scene); a batch's
+    // tables sit one after another in one key space of 32 bits.
+    if ((int64_t)cfg->maxNeighbours * (int64_t)n > (int64_t)(scenes ? UINT32_MAX : INT_MAX))
+        return AKUA_ERR_TOO_LARGE;
     akua_pbf* s = new (std::nothrow) akua_pbf();
     if (!s) return AKUA_ERR_OUT_OF_MEMORY;
     s->n = n;
     s->cfg = *cfg;
     s->corr = *corr;
-    s->table_size = (uint32_t)(cfg->maxNeighbours * n);
+    s->table_size = (uint32_t)((int64_t)cfg->maxNeighbours * n);
     s->table_alloc = s->table_size;
     cudaGetDevice(&s->device);
+    std::vector<uint16_t> sid;
+    if (scenes) {
+        s->scenes.assign(scenes, scenes + num_scenes);
+        uint32_t first = 0;
+        sid.resize((size_t)n);
+        for (int k = 0; k < num_scenes; ++k) {
+            s->scene_first.push_back(first);
+            for (int32_t q = 0; q < scenes[k].numParticles; ++q) sid[first + q] = (uint16_t)k;
+            first += (uint32_t)scenes[k].numParticles;
+        }
+        while ((1 << s->scene_bits) < num_scenes) ++s->scene_bits;
+    }
     const size_t N = (size_t)n;
     const size_t cap = (size_t)cfg->maxNeighbours;
     cudaError_t e = cudaSuccess;
     auto chk = [&](cudaError_t r) {
         if (e == cudaSuccess) e = r;
     };
-    chk(dalloc(s, &s->d_params, 1));
+    chk(dalloc(s, &s->d_params, scenes ? (size_t)num_scenes : 1));
+    if (scenes) {
+        chk(dalloc(s, &s->scene_of, N));
+        if (e == cudaSuccess)
+            e = cudaMemcpy(s->scene_of, sid.data(), sizeof(uint16_t) * N, cudaMemcpyHostToDevice);
+    }
     chk(dalloc(s, &s->x4, N)); chk(dalloc(s, &s->v4, N)); chk(dalloc(s, &s->col4, N));
     chk(dalloc(s, &s->size, N)); chk(dalloc(s, &s->rref, N));
     chk(dalloc(s, &s->rho, N)); chk(dalloc(s, &s->lam, N)); chk(dalloc(s, &s->dp4, N));
@@ -554,6 +630,49 @@ int akua_pbf_create(int32_t n, const akua_pbf_config* cfg, const akua_lambda_cor
     return AKUA_OK;
 }
 
+}  // namespace
+
+extern "C" {
+
+int akua_pbf_create(int32_t n, const akua_pbf_config* cfg, const akua_lambda_corr_params* corr,
+                    akua_pbf** out) {
+    return create_solver(n, cfg, corr, nullptr, 0, out);
+}
+
+int akua_pbf_create_batch(int32_t num_scenes, const akua_scene_desc* scenes,
+                          const akua_pbf_config* cfg, const akua_lambda_corr_params* corr,
+                          akua_pbf** out) {
+    if (out) *out = nullptr;
+    if (!scenes || num_scenes <= 0 || num_scenes > 65535) return AKUA_ERR_INVALID_ARGUMENT;
+    int64_t total = 0;
+    for (int k = 0; k < num_scenes; ++k) {
+        const akua_scene_desc& d = scenes[k];
+        if (d.numParticles <= 0 || !finite3(d.gravity) || !finite3(d.boxMin) || !finite3(d.boxMax))
+            return AKUA_ERR_INVALID_ARGUMENT;
+        if (cfg && (int64_t)cfg->maxNeighbours * d.numParticles > (int64_t)INT_MAX)
+            return AKUA_ERR_TOO_LARGE;
+        total += d.numParticles;
+    }
+    if (total > (int64_t)INT_MAX) return AKUA_ERR_TOO_LARGE;
+    return create_solver((int32_t)total, cfg, corr, scenes, num_scenes, out);
+}
+
+int akua_pbf_step_batch(akua_pbf* s, float dt) {
+    if (!s || s->scenes.empty()) return AKUA_ERR_INVALID_ARGUMENT;
+    if (!s->attached) return AKUA_ERR_NOT_ATTACHED;
+    DeviceGuard g(s->device);
+    return do_step(s, s->attached, s->stride, false, dt, nullptr, nullptr);
+}
+
+int akua_pbf_set_scene(akua_pbf* s, int32_t scene, const akua_scene_desc* desc) {
+    if (!s || !desc || scene < 0 || scene >= (int32_t)s->scenes.size()) return AKUA_ERR_INVALID_ARGUMENT;
+    if (desc->numParticles != s->scenes[scene].numParticles || !finite3(desc->gravity) ||
+        !finite3(desc->boxMin) || !finite3(desc->boxMax))
+        return AKUA_ERR_INVALID_ARGUMENT;
+    s->scenes[scene] = *desc;
+    return AKUA_OK;
+}
+
 int akua_pbf_destroy(akua_pbf* s) {
     if (!s) return AKUA_ERR_INVALID_ARGUMENT;
     DeviceGuard g(s->device);
@@ -575,7 +694,7 @@ int akua_pbf_attach_particles(akua_pbf* s, void* dev, size_t stride) {
 }
 
 int akua_pbf_step(akua_pbf* s, float dt, const float bmin[3], const float bmax[3]) {
-    if (!s) return AKUA_ERR_INVALID_ARGUMENT;
+    if (!s || !s->scenes.empty()) return AKUA_ERR_INVALID_ARGUMENT;  // batches: akua_pbf_step_batch
     if (!s->attached) return AKUA_ERR_NOT_ATTACHED;
     DeviceGuard g(s->device);
     return do_step(s, s->attached, s->stride, false, dt, bmin, bmax);
@@ -583,7 +702,7 @@ int akua_pbf_step(akua_pbf* s, float dt, const float bmin[3], const float bmax[3
 
 int akua_pbf_step_host(akua_pbf* s, void* host, size_t stride, float dt, const float bmin[3],
                        const float bmax[3]) {
-    if (!s || !host || stride < sizeof(akua_particle) || stride % 4 != 0)
+    if (!s || !host || stride < sizeof(akua_particle) || stride % 4 != 0 || !s->scenes.empty())
         return AKUA_ERR_INVALID_ARGUMENT;
     DeviceGuard g(s->device);
     const size_t bytes = (size_t)s->n * stride;
@@ -614,7 +733,7 @@ int akua_pbf_step_host(akua_pbf* s, void* host, size_t stride, float dt, const f
 }
 
 int akua_pbf_set_gravity(akua_pbf* s, const float g[3]) {
-    if (!s || !finite3(g)) return AKUA_ERR_INVALID_ARGUMENT;
+    if (!s || !finite3(g) || !s->scenes.empty()) return AKUA_ERR_INVALID_ARGUMENT;
     for (int a = 0; a < 3; ++a) s->cfg.gravity[a] = g[a];
     return AKUA_OK;
 }
@@ -636,7 +755,7 @@ int akua_pbf_set_solver_iterations(akua_pbf* s, int32_t iterations) {
 }
 
 int akua_pbf_set_table_size(akua_pbf* s, int32_t table_size) {
-    if (!s || table_size <= 0) return AKUA_ERR_INVALID_ARGUMENT;
+    if (!s || table_size <= 0 || !s->scenes.empty()) return AKUA_ERR_INVALID_ARGUMENT;
     DeviceGuard g(s->device);
     if ((uint32_t)table_size > s->table_alloc) {
         cudaError_t e = cudaStreamSynchronize(s->stream);
@@ -729,7 +848,7 @@ int akua_pbf_read_debug(akua_pbf* s, int32_t what, void* dst, size_t bytes) {
             return cuda_status(e);
         }
         akua::k_export<<<grid_for(s->n, akua::kIoBlock), akua::kIoBlock, 0, s->stream>>>(
-            tmp, sizeof(akua_particle), s->n, s->r2i, s->kr, s->x4, s->v4, s->vstar4, s->dp4,
+            s->d_params, tmp, sizeof(akua_particle), s->n, s->r2i, s->kr, s->x4, s->v4, s->vstar4, s->dp4,
             s->om4, s->rho, s->lam, s->col4, s->size, nullptr, nullptr);
         e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaMemcpyAsync(dst, tmp, need, cudaMemcpyDeviceToHost, s->stream);

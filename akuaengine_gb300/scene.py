@@ -98,6 +98,61 @@ def double_dam_break(block=(200, 100, 200), box_widths=(6.0, 2.0, 2.0), h=0.1, s
                  {"block": tuple(block), "box_widths": tuple(box_widths), "seed": seed})
 
 
+@dataclass
+class SceneBatch:
+    """Independent scenes stepped by one batch solver: records of scene k at
+    [first[k], first[k] + n_k) of `particles`."""
+    particles: np.ndarray
+    scenes: list            # per scene: dict(numParticles, gravity, box_min, box_max, seed, block)
+    dt: float
+    name: str
+
+    @property
+    def n(self) -> int:
+        return int(self.particles.shape[0])
+
+    @property
+    def first(self) -> list:
+        out, f = [], 0
+        for d in self.scenes:
+            out.append(f)
+            f += d["numParticles"]
+        return out
+
+    def scene(self, k: int) -> Scene:
+        """Scene k alone (its own records, box and gravity in `meta`)."""
+        d, f = self.scenes[k], self.first[k]
+        return Scene(self.particles[f:f + d["numParticles"]].copy(), d["box_min"], d["box_max"],
+                     self.dt, "%s[%d]" % (self.name, k), {"gravity": d["gravity"]})
+
+
+def batched_dam_breaks(count=256, n_min=2000, n_max=64000, h=0.1, seed=0, dt=0.0083,
+                       jitter_frac=0.01) -> SceneBatch:
+    """`count` independent dam breaks: particle counts log-uniform in [n_min, n_max], block
+    aspect ratios uniform in [0.5, 2] per axis, gravity magnitude uniform in [5, 15] (along -y),
+    box extents 2-4x the block's per axis, lattice spacing 0.5h with jitter +-jitter_frac*h, one
+    seed per scene."""
+    rng = np.random.default_rng(seed)
+    spacing = F32(0.5 * h)
+    parts, scenes = [], []
+    for k in range(count):
+        target = float(np.exp(rng.uniform(np.log(n_min), np.log(n_max))))
+        aspect = rng.uniform(0.5, 2.0, 3)
+        c = (target / float(np.prod(aspect))) ** (1.0 / 3.0)
+        block = [max(2, int(round(a * c))) for a in aspect]
+        g = float(rng.uniform(5.0, 15.0))
+        factor = rng.uniform(2.0, 4.0, 3)
+        box_max = tuple(float(F32((b + 2) * float(spacing) * f)) for b, f in zip(block, factor))
+        origin = (float(spacing),) * 3
+        sseed = int(rng.integers(0, 2 ** 31))
+        p = lattice_block(block, spacing, origin, jitter=float(F32(jitter_frac * h)), seed=sseed)
+        parts.append(p)
+        scenes.append({"numParticles": int(p.shape[0]), "gravity": (0.0, -g, 0.0),
+                       "box_min": (0.0, 0.0, 0.0), "box_max": box_max, "seed": sseed,
+                       "block": tuple(block)})
+    return SceneBatch(np.concatenate(parts), scenes, dt, "batched_%d" % count)
+
+
 # Workloads of the benchmark configurations (sizes and parameters; seeded synthetic data).
 def workload(name: str, seed: int = 0) -> Scene:
     if name == "dam_break_27k":

@@ -250,3 +250,56 @@ class PBFSolver:
             self.close()
         except Exception:
             pass
+
+
+class BatchSolver(PBFSolver):
+    """Many independent scenes in one solver (C ABI akua_pbf_create_batch): every kernel of a step
+    covers all scenes, and each scene's records come out as if it were stepped alone.  `scenes`:
+    dicts (or objects) with numParticles, gravity, box_min, box_max."""
+
+    def __init__(self, scenes, config: PBFConfig | None = None,
+                 corrParams: LambdaCorrParams | None = None, *, options: int = 0, stream=None):
+        self._lib = load_library()
+        self.config = dataclasses.replace(config) if config is not None else PBFConfig()
+        self.corrParams = (dataclasses.replace(corrParams) if corrParams is not None
+                           else LambdaCorrParams())
+        self._cfg = self.config.to_c()
+        self._corr = self.corrParams.to_c()
+        descs = (_abi.CSceneDesc * len(scenes))()
+        for k, d in enumerate(scenes):
+            descs[k] = _scene_desc(d)
+        self.scenes = list(scenes)
+        self.numParticles = int(sum(_get(d, "numParticles") for d in scenes))
+        h = ctypes.c_void_p()
+        check(self._lib.akua_pbf_create_batch(len(scenes), descs, ctypes.byref(self._cfg),
+                                              ctypes.byref(self._corr), ctypes.byref(h)),
+              "akua_pbf_create_batch")
+        self._h = h
+        self._attached = None
+        if options:
+            self.set_options(options)
+        if stream is not None:
+            self.set_stream(stream)
+
+    def step(self, particles, deltaTime: float) -> None:
+        self.attach(as_particle_buffer(particles))
+        check(self._lib.akua_pbf_step_batch(self._h, float(deltaTime)), "akua_pbf_step_batch")
+
+    def set_scene(self, k: int, scene) -> None:
+        d = _scene_desc(scene)
+        check(self._lib.akua_pbf_set_scene(self._h, int(k), ctypes.byref(d)), "akua_pbf_set_scene")
+        self.scenes[k] = scene
+
+
+def _get(d, name):
+    return d[name] if isinstance(d, dict) else getattr(d, name)
+
+
+def _scene_desc(d) -> "_abi.CSceneDesc":
+    c = _abi.CSceneDesc()
+    c.numParticles = int(_get(d, "numParticles"))
+    for a in range(3):
+        c.gravity[a] = float(_get(d, "gravity")[a])
+        c.boxMin[a] = float(_get(d, "box_min")[a])
+        c.boxMax[a] = float(_get(d, "box_max")[a])
+    return c

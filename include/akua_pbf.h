@@ -186,6 +186,30 @@ int akua_pbf_profile_end(akua_pbf* solver, akua_kernel_time* out, int32_t capaci
 int akua_sort_pairs_noalloc(const uint32_t* keysIn, const uint32_t* valsIn, uint32_t* keysOut,
                             uint32_t* valsOut, int32_t n, int32_t keyBits, void* cudaStream);
 
+/* ---- Batches of independent scenes.  No counterpart in the reference (one solver per scene). ---
+ * One handle steps many scenes at once: their particle records lie one after another in the
+ * attached array (scene k at records [first_k, first_k + numParticles_k)), every kernel of a step
+ * covers all of them, and each scene's result is bit-identical to stepping it alone with its own
+ * solver (same hash table size maxNeighbours * N_k, box and gravity): the hash keys of scene k
+ * are offset by maxNeighbours * first_k, so one sort orders the batch by (scene, hash) and each
+ * scene's records come back sorted within its own range.  A batch handle takes
+ * akua_pbf_step_batch / akua_pbf_set_scene in place of akua_pbf_step / akua_pbf_step_host /
+ * akua_pbf_set_gravity / akua_pbf_set_table_size (those return AKUA_ERR_INVALID_ARGUMENT). */
+typedef struct akua_scene_desc {
+    int32_t numParticles;
+    float gravity[3];
+    float boxMin[3];
+    float boxMax[3];
+} akua_scene_desc;
+/* At most 65535 scenes; shared PBFConfig / LambdaCorrParams. */
+int akua_pbf_create_batch(int32_t numScenes, const akua_scene_desc* scenes,
+                          const akua_pbf_config* config, const akua_lambda_corr_params* corr,
+                          akua_pbf** out);
+/* One step of every scene of the batch over the attached records; asynchronous. */
+int akua_pbf_step_batch(akua_pbf* solver, float deltaTime);
+/* Changes scene `scene`'s gravity and box (numParticles must stay the same). */
+int akua_pbf_set_scene(akua_pbf* solver, int32_t scene, const akua_scene_desc* desc);
+
 /* ---- Learned lambda warm start.  No counterpart in the reference. ----------------------------
  * A network of 8 inputs, three hidden layers of 64 SiLU units and one output, BF16 weights and
  * activations on the tensor cores with FP32 accumulation, trained on the GPU.  It predicts, from
