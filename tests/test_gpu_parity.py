@@ -235,6 +235,17 @@ def test_fast_one_step_1m_full_size():
     assert_close_fast(g, o)
 
 
+def test_exact_one_step_8m_double_dam_break():
+    """8M particles in two blocks (the table is 128 N = 1.024e9 buckets, as the reference's
+    formula gives): one step, grid and every record bit-exact against the oracle."""
+    sc = scene.workload("double_dam_break_8m", seed=0)
+    cfg, corr = bench_params()
+    g, ge = run_gpu(sc, cfg, corr, 1, ak.OPT_EXACT_MATH)
+    o, oe = run_oracle(sc, cfg, corr, 1)
+    assert_grid_equal(ge, oe, cfg.maxNeighbours)
+    assert_records_bitexact(g, o)
+
+
 def test_fast_error_against_fp64_oracle():
     """FP32 error of one GPU step measured against the same equations in double precision."""
     sc = scene.workload("dam_break_27k", seed=3)
