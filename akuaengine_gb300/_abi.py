@@ -17,6 +17,7 @@ AKUA_ERR_OUT_OF_MEMORY = -3
 AKUA_ERR_NOT_ATTACHED = -4
 AKUA_ERR_DEVICE_CHECK = -5
 AKUA_ERR_TOO_LARGE = -6
+AKUA_ERR_CORRUPT = -7
 
 OPT_EXACT_MATH = 0x1
 OPT_RESIDENT = 0x2
@@ -27,11 +28,14 @@ MLP_HIDDEN = 64
 MLP_PARAMS = 8961
 MLP_NORM = 18
 
+STATE_LAMBDA_SUMS = 0x1
+
 DEBUG_HASHES = 1
 DEBUG_ORDER = 2
 DEBUG_NEIGHBOUR_COUNTS = 3
 DEBUG_NEIGHBOURS = 4
 DEBUG_PARTICLES = 5
+DEBUG_LAMBDA_SUMS = 6
 
 FLAG_CAP_REACHED = 1
 FLAG_BAD_TABLE = 2
@@ -68,6 +72,17 @@ class CCorr(ctypes.Structure):
 class CSceneDesc(ctypes.Structure):
     _fields_ = [("numParticles", ctypes.c_int32), ("gravity", ctypes.c_float * 3),
                 ("boxMin", ctypes.c_float * 3), ("boxMax", ctypes.c_float * 3)]
+
+
+class CStateHeader(ctypes.Structure):
+    _fields_ = [("magic", ctypes.c_char * 8), ("version", ctypes.c_uint32),
+                ("recordBytes", ctypes.c_uint32), ("numParticles", ctypes.c_int64),
+                ("step", ctypes.c_int64), ("config", CConfig), ("corr", CCorr),
+                ("boxMin", ctypes.c_float * 3), ("boxMax", ctypes.c_float * 3),
+                ("deltaTime", ctypes.c_float), ("tableSize", ctypes.c_uint32),
+                ("sections", ctypes.c_uint32), ("numScenes", ctypes.c_int32),
+                ("crc32", ctypes.c_uint32), ("options", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint8 * 112)]
 
 
 class CStats(ctypes.Structure):
@@ -133,6 +148,12 @@ _SIGS = {
                                             ctypes.POINTER(ctypes.c_int32)]),
     "akua_sort_pairs_noalloc": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int32, ctypes.c_int32, _P]),
     "akua_pbf_set_solver_iterations": (ctypes.c_int, [_P, ctypes.c_int32]),
+    "akua_state_init_header": (None, [ctypes.POINTER(CStateHeader)]),
+    "akua_state_save": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(CStateHeader), _P, _P, _P]),
+    "akua_state_read_header": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(CStateHeader)]),
+    "akua_state_load": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(CStateHeader), _P,
+                                       ctypes.c_int64, _P, _P, ctypes.c_int32]),
+    "akua_pbf_set_lambda_sums": (ctypes.c_int, [_P, _P, ctypes.c_int64]),
     "akua_pbf_create_batch": (ctypes.c_int, [ctypes.c_int32, ctypes.POINTER(CSceneDesc),
                                              ctypes.POINTER(CConfig), ctypes.POINTER(CCorr),
                                              ctypes.POINTER(_P)]),

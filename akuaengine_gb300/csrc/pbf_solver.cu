@@ -830,7 +830,8 @@ int akua_pbf_read_debug(akua_pbf* s, int32_t what, void* dst, size_t bytes) {
     switch (what) {
         case AKUA_DEBUG_HASHES:
         case AKUA_DEBUG_ORDER:
-        case AKUA_DEBUG_NEIGHBOUR_COUNTS: need = N * 4; break;
+        case AKUA_DEBUG_NEIGHBOUR_COUNTS:
+        case AKUA_DEBUG_LAMBDA_SUMS: need = N * 4; break;
         case AKUA_DEBUG_NEIGHBOURS: need = N * cap * 4; break;
         case AKUA_DEBUG_PARTICLES: need = N * sizeof(akua_particle); break;
         default: return AKUA_ERR_INVALID_ARGUMENT;
@@ -839,6 +840,13 @@ int akua_pbf_read_debug(akua_pbf* s, int32_t what, void* dst, size_t bytes) {
     cudaError_t e = cudaStreamSynchronize(s->stream);
     if (e != cudaSuccess) return cuda_status(e);
     if (what == AKUA_DEBUG_HASHES) return cuda_status(cudaMemcpy(dst, s->kr, need, cudaMemcpyDeviceToHost));
+    if (what == AKUA_DEBUG_LAMBDA_SUMS) {
+        if (!s->lacc_ref) {
+            std::memset(dst, 0, need);
+            return AKUA_OK;
+        }
+        return cuda_status(cudaMemcpy(dst, s->lacc_ref, need, cudaMemcpyDeviceToHost));
+    }
     if (what == AKUA_DEBUG_ORDER) return cuda_status(cudaMemcpy(dst, s->order, need, cudaMemcpyDeviceToHost));
     if (what == AKUA_DEBUG_PARTICLES) {
         char* tmp = nullptr;
@@ -991,6 +999,17 @@ int akua_pbf_set_lambda_tracking(akua_pbf* s, int32_t enabled) {
     return AKUA_OK;
 }
 
+int akua_pbf_set_lambda_sums(akua_pbf* s, const float* host, int64_t count) {
+    if (!s || !host || count != (int64_t)s->n) return AKUA_ERR_INVALID_ARGUMENT;
+    DeviceGuard g(s->device);
+    cudaError_t e = ensure_learn_buffers(s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(s->lacc_ref, host, sizeof(float) * (size_t)count, cudaMemcpyHostToDevice);
+    s->state_valid = false;  // the next step re-imports records and sums together
+    return cuda_status(e);
+}
+
 int akua_pbf_density_error(akua_pbf* s, float* max_error, float* mean_abs_error) {
     if (!s || !max_error || !mean_abs_error) return AKUA_ERR_INVALID_ARGUMENT;
     if (!s->stepped) return AKUA_ERR_NOT_ATTACHED;
@@ -1026,6 +1045,7 @@ const char* akua_pbf_status_string(int status) {
         case AKUA_ERR_NOT_ATTACHED: return "no particle buffer attached";
         case AKUA_ERR_DEVICE_CHECK: return "device-side check failed";
         case AKUA_ERR_TOO_LARGE: return "size exceeds the entry point's limit";
+        case AKUA_ERR_CORRUPT: return "state file failed its checksum";
         default: return "unknown status";
     }
 }

@@ -173,6 +173,13 @@ class PBFSolver:
         check(self._lib.akua_pbf_set_lambda_tracking(self._h, int(bool(enabled))),
               "akua_pbf_set_lambda_tracking")
 
+    def set_lambda_sums(self, sums) -> None:
+        """The per-particle lambda sums the next step reads as the previous step's (record
+        order), e.g. from a state file."""
+        a = np.ascontiguousarray(sums, dtype=np.float32)
+        check(self._lib.akua_pbf_set_lambda_sums(self._h, a.ctypes.data_as(ctypes.c_void_p),
+                                                 a.size), "akua_pbf_set_lambda_sums")
+
     def density_error(self) -> tuple[float, float]:
         """(max_i max(rho_i/rho0 - 1, 0), mean_i |rho_i/rho0 - 1|) at the last step's end."""
         mx, mean = ctypes.c_float(), ctypes.c_float()
@@ -225,6 +232,8 @@ class PBFSolver:
         n = self.numParticles
         if what == _abi.DEBUG_PARTICLES:
             out = np.zeros(n, dtype=PARTICLE_DTYPE)
+        elif what == _abi.DEBUG_LAMBDA_SUMS:
+            out = np.zeros(n, dtype=np.float32)
         elif what == _abi.DEBUG_NEIGHBOURS:
             out = np.zeros((n, self.config.maxNeighbours), dtype=np.uint32)
         else:

@@ -29,6 +29,7 @@ extern "C" {
 #define AKUA_ERR_NOT_ATTACHED (-4)  /* step before a particle buffer was attached */
 #define AKUA_ERR_DEVICE_CHECK (-5)  /* a device-side consistency check failed */
 #define AKUA_ERR_TOO_LARGE (-6)     /* a size exceeds a fixed limit of the called entry point */
+#define AKUA_ERR_CORRUPT (-7)       /* a state file failed its checksum */
 
 /* Options (akua_pbf_set_options). */
 #define AKUA_PBF_OPT_EXACT_MATH 0x1u /* IEEE sqrt/divide in every pair term (bit-reproducible) */
@@ -94,6 +95,7 @@ typedef struct akua_pbf_stats {
 #define AKUA_DEBUG_NEIGHBOUR_COUNTS 3 /* uint32[N] */
 #define AKUA_DEBUG_NEIGHBOURS 4       /* uint32[N * maxNeighbours], row i holds particle i's list */
 #define AKUA_DEBUG_PARTICLES 5        /* akua_particle[N]: the solver's current state */
+#define AKUA_DEBUG_LAMBDA_SUMS 6      /* float[N]: last step's accumulated lambda, record order */
 
 /* Reference defaults of PBFConfig / LambdaCorrParams (PBFConfig.h:10-29). */
 void akua_pbf_default_config(akua_pbf_config* config, akua_lambda_corr_params* corr);
@@ -209,6 +211,49 @@ int akua_pbf_create_batch(int32_t numScenes, const akua_scene_desc* scenes,
 int akua_pbf_step_batch(akua_pbf* solver, float deltaTime);
 /* Changes scene `scene`'s gravity and box (numParticles must stay the same). */
 int akua_pbf_set_scene(akua_pbf* solver, int32_t scene, const akua_scene_desc* desc);
+
+/* ---- State files.  No counterpart in the reference (its scene is rebuilt in code each run). ----
+ * A file holds the particle records of a simulation and what resuming it needs: the solver
+ * parameters, box, time step, step count and table size, optionally the per-particle lambda sums
+ * (warm start) and the scenes of a batch.  Records plus parameters determine every later step, so
+ * a run resumed from a file continues bit for bit.  Layout: a 256-byte header, the records, the
+ * lambda sums (float[N]) if sections & AKUA_STATE_LAMBDA_SUMS, the scene descriptors if
+ * numScenes > 0; crc32 (IEEE, as zlib's) covers everything after the header. */
+#define AKUA_STATE_VERSION 1
+#define AKUA_STATE_HEADER_BYTES 256
+#define AKUA_STATE_LAMBDA_SUMS 0x1u
+typedef struct akua_state_header {
+    char magic[8];                /* "AKUAPBF\0" */
+    uint32_t version;             /* AKUA_STATE_VERSION */
+    uint32_t recordBytes;         /* 108 */
+    int64_t numParticles;
+    int64_t step;                 /* steps simulated before this state */
+    akua_pbf_config config;
+    akua_lambda_corr_params corr;
+    float boxMin[3];
+    float boxMax[3];
+    float deltaTime;
+    uint32_t tableSize;
+    uint32_t sections;            /* AKUA_STATE_* bits */
+    int32_t numScenes;            /* 0: one scene */
+    uint32_t crc32;               /* written by akua_state_save */
+    uint32_t options;             /* AKUA_PBF_OPT_* of the run */
+    uint8_t reserved[112];
+} akua_state_header;
+/* Zeroes `header` and fills magic, version and recordBytes. */
+void akua_state_init_header(akua_state_header* header);
+/* Writes a state file; lambdaSums must be given exactly when the header's sections say so, and
+ * scenes exactly when numScenes > 0.  Host memory only. */
+int akua_state_save(const char* path, const akua_state_header* header, const void* records,
+                    const float* lambdaSums, const akua_scene_desc* scenes);
+int akua_state_read_header(const char* path, akua_state_header* header);
+/* Reads a state file into host memory (records: capacity records; lambdaSums may be NULL to skip
+ * them; scenes: sceneCapacity descriptors); AKUA_ERR_CORRUPT when the checksum does not match. */
+int akua_state_load(const char* path, akua_state_header* header, void* records, int64_t capacity,
+                    float* lambdaSums, akua_scene_desc* scenes, int32_t sceneCapacity);
+/* Sets the per-particle lambda sums the next step reads as "the previous step's" (record order;
+ * the counterpart of AKUA_DEBUG_LAMBDA_SUMS, for resuming a warm-started run). */
+int akua_pbf_set_lambda_sums(akua_pbf* solver, const float* hostSums, int64_t count);
 
 /* ---- Learned lambda warm start.  No counterpart in the reference. ----------------------------
  * A network of 8 inputs, three hidden layers of 64 SiLU units and one output, BF16 weights and
