@@ -85,6 +85,12 @@ class CStateHeader(ctypes.Structure):
                 ("reserved", ctypes.c_uint8 * 112)]
 
 
+class CCamera(ctypes.Structure):
+    _fields_ = [("position", ctypes.c_float * 3), ("gaze", ctypes.c_float * 3),
+                ("up", ctypes.c_float * 3), ("fovDegrees", ctypes.c_float),
+                ("nearZ", ctypes.c_float), ("farZ", ctypes.c_float)]
+
+
 class CStats(ctypes.Structure):
     _fields_ = [
         ("numParticles", ctypes.c_int32),
@@ -148,6 +154,12 @@ _SIGS = {
                                             ctypes.POINTER(ctypes.c_int32)]),
     "akua_sort_pairs_noalloc": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int32, ctypes.c_int32, _P]),
     "akua_pbf_set_solver_iterations": (ctypes.c_int, [_P, ctypes.c_int32]),
+    "akua_camera_default": (None, [ctypes.POINTER(CCamera)]),
+    "akua_camera_matrices": (ctypes.c_int, [ctypes.POINTER(CCamera), ctypes.c_float, _P, _P, _P]),
+    "akua_splat_create": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(_P)]),
+    "akua_splat_destroy": (ctypes.c_int, [_P]),
+    "akua_splat_render": (ctypes.c_int, [_P, _P, ctypes.c_size_t, ctypes.c_int32,
+                                         ctypes.POINTER(CCamera), _P, _P]),
     "akua_state_init_header": (None, [ctypes.POINTER(CStateHeader)]),
     "akua_state_save": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(CStateHeader), _P, _P, _P]),
     "akua_state_read_header": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(CStateHeader)]),

@@ -31,7 +31,8 @@ def nvcc_path() -> str:
 
 def sources() -> list[str]:
     return [os.path.join(CSRC, "pbf_solver.cu"), os.path.join(CSRC, "sort_noalloc.cu"),
-            os.path.join(CSRC, "mlp.cu"), os.path.join(CSRC, "state_io.cpp")]
+            os.path.join(CSRC, "mlp.cu"), os.path.join(CSRC, "state_io.cpp"),
+            os.path.join(CSRC, "splat.cu")]
 
 
 def headers() -> list[str]:

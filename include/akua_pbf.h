@@ -255,6 +255,34 @@ int akua_state_load(const char* path, akua_state_header* header, void* records, 
  * the counterpart of AKUA_DEBUG_LAMBDA_SUMS, for resuming a warm-started run). */
 int akua_pbf_set_lambda_sums(akua_pbf* solver, const float* hostSums, int64_t count);
 
+/* ---- Headless point-splat renderer.  Replaces the reference's GL particle pass
+ * (assets/shaders/fluidParticle.vert/.frag, src/Rendering/Renderer.cpp:29-50) with CUDA kernels
+ * writing an RGBA8 image: points of size Particle::size / distance, a round splat with
+ * colour * exp(-3 r^2) (r = distance from the splat centre in units of its size), depth test
+ * LESS, no blending, clear colour (0.15, 0.15, 0.18, 1). */
+typedef struct akua_camera {
+    float position[3];
+    float gaze[3];      /* view direction */
+    float up[3];        /* world up */
+    float fovDegrees;   /* vertical field of view */
+    float nearZ;
+    float farZ;
+} akua_camera;
+/* The reference's camera at start-up (CameraConfig.h:8-16, Application.cpp:17-18). */
+void akua_camera_default(akua_camera* camera);
+/* Column-major view (lookAt(position, position + gaze, up)), projection (perspective, depth in
+ * [-1, 1]) and projection * view; any output may be NULL. */
+int akua_camera_matrices(const akua_camera* camera, float aspect, float* view, float* projection,
+                         float* viewProjection);
+typedef struct akua_splat akua_splat;
+int akua_splat_create(int32_t width, int32_t height, akua_splat** out);
+int akua_splat_destroy(akua_splat* renderer);
+/* Renders n particle records (device memory, strideBytes apart) into deviceRGBA (width * height
+ * pixels, R in the low byte, row 0 at the top); asynchronous on cudaStream. */
+int akua_splat_render(akua_splat* renderer, const void* deviceParticles, size_t strideBytes,
+                      int32_t n, const akua_camera* camera, uint32_t* deviceRGBA,
+                      void* cudaStream);
+
 /* ---- Learned lambda warm start.  No counterpart in the reference. ----------------------------
  * A network of 8 inputs, three hidden layers of 64 SiLU units and one output, BF16 weights and
  * activations on the tensor cores with FP32 accumulation, trained on the GPU.  It predicts, from
