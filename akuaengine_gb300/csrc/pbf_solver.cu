@@ -891,9 +891,11 @@ int akua_pbf_read_debug(akua_pbf* s, int32_t what, void* dst, size_t bytes) {
 int akua_pbf_kernels_per_step(akua_pbf* s) {
     if (!s) return AKUA_ERR_INVALID_ARGUMENT;
     if (s->body_launches == 0) return AKUA_ERR_INVALID_ARGUMENT;  // no step issued yet
-    // parameter upload + import (when it runs) + the body
+    // parameter upload (one launch per chunk of scenes) + import (when it runs) + the body
     const bool import = !(s->options & AKUA_PBF_OPT_RESIDENT);
-    return 1 + (import ? 1 : 0) + s->body_launches;
+    const int uploads =
+        s->scenes.empty() ? 1 : (int)((s->scenes.size() + akua::kParamChunk - 1) / akua::kParamChunk);
+    return uploads + (import ? 1 : 0) + s->body_launches;
 }
 
 int akua_pbf_profile_begin(akua_pbf* s, int32_t max_steps) {
