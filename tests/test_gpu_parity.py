@@ -124,6 +124,23 @@ def test_capacity_truncation_bitexact():
     assert_records_bitexact(g, o)
 
 
+@pytest.mark.parametrize("cap", [128, 100, 200])
+@pytest.mark.parametrize("table_size", [None, 4096])
+def test_long_lists_bitexact(cap, table_size):
+    """A lattice at 0.3h gives ~150 neighbours: lists run past the walk's 64-entry stage (the
+    overflow pass) and, for cap 100/128, past the capacity; with a small table the long lists also
+    hold duplicated and foreign-cell candidates."""
+    p = scene.lattice_block((16, 16, 16), 0.03, (1.0, 1.0, 1.0), jitter=0.001, seed=7)
+    sc = scene.Scene(p, (0.0, 0.0, 0.0), (3.0, 3.0, 3.0), 0.0083, "dense")
+    cfg = PBFConfig(maxNeighbours=cap)
+    corr = LambdaCorrParams()
+    g, ge = run_gpu(sc, cfg, corr, 1, ak.OPT_EXACT_MATH, table_size=table_size)
+    o, oe = run_oracle(sc, cfg, corr, 1, table_size=table_size)
+    assert ge["cnt"].max() > 64
+    assert_grid_equal(ge, oe, cfg.maxNeighbours)
+    assert_records_bitexact(g, o)
+
+
 def test_small_table_collisions_bitexact():
     """A 4096-entry table makes many cells share a bucket (duplicated and foreign candidates)."""
     sc = scene.dam_break((12, 12, 12), (3.0, 3.0, 3.0), seed=4)
