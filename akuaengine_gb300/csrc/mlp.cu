@@ -54,10 +54,10 @@ int launch_grad(akua_mlp* m, const float* feat, const float* target, int32_t n, 
 namespace akua::mlp {
 // Used by the step (pbf_solver.cu): the forward pass writing lambda (and its running sum).
 int enqueue_forward(const akua_mlp* m, const float* feat, int n, float* out, float* out2,
-                    cudaStream_t st) {
+                    float* out4, cudaStream_t st) {
     const int tiles = (n + kTile - 1) / kTile;
     const int grid = std::max(1, std::min(tiles, 5 * m->sms));  // 5 x 40 KB of shared memory
-    k_mlp_forward<<<grid, kThreads, 0, st>>>(m->params, m->norm, feat, n, out, out2, m->err);
+    k_mlp_forward<<<grid, kThreads, 0, st>>>(m->params, m->norm, feat, n, out, out2, out4, m->err);
     return status_of(cudaGetLastError());
 }
 }  // namespace akua::mlp
@@ -153,7 +153,7 @@ int akua_mlp_forward(akua_mlp* m, const float* features, float* out, int32_t n, 
     if (!m || n < 0 || (n > 0 && (!features || !out))) return AKUA_ERR_INVALID_ARGUMENT;
     if (n == 0) return AKUA_OK;
     Guard g(m->device);
-    return akua::mlp::enqueue_forward(m, features, n, out, nullptr, (cudaStream_t)stream);
+    return akua::mlp::enqueue_forward(m, features, n, out, nullptr, nullptr, (cudaStream_t)stream);
 }
 
 int akua_mlp_gradient(akua_mlp* m, const float* features, const float* targets, int32_t n,

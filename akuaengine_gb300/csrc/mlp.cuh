@@ -176,11 +176,12 @@ __device__ __forceinline__ void load_features(const float* __restrict__ feat, in
 }
 
 // Features (n x 8, FP32) -> out2[i] = the network's estimate p_i (output * out_scale) and
-// out[i] = lambda0_i + blend * (p_i - lambda0_i), lambda0 = feature 3 (blend 1: out = p).
+// out[i] = lambda0_i + blend * (p_i - lambda0_i), lambda0 = feature 3 (blend 1: out = p); the
+// latter also into out4[4 i] when given.
 __global__ void __launch_bounds__(kThreads)
     k_mlp_forward(const float* __restrict__ params, const float* __restrict__ norm,
                   const float* __restrict__ feat, int n, float* __restrict__ out,
-                  float* __restrict__ out2, uint32_t* __restrict__ err) {
+                  float* __restrict__ out2, float* __restrict__ out4, uint32_t* __restrict__ err) {
     __shared__ FwdSmem S;
     const int t = threadIdx.x, warp = t >> 5;
     stage_weight(S.w1, params + kW1, kIn, kInPad, false, t);
@@ -264,8 +265,10 @@ __global__ void __launch_bounds__(kThreads)
         const float y = output_layer(lane, S.b3, S.w4, S.b4);
         if (i < n) {
             const float o = y * S.norm[2 * kIn];
-            out[i] = blend == 1.0f ? o : __fmaf_rn(blend, o - lam0, lam0);
+            const float used = blend == 1.0f ? o : __fmaf_rn(blend, o - lam0, lam0);
+            out[i] = used;
             if (out2) out2[i] = o;
+            if (out4) out4[4 * (size_t)i] = used;  // a float4 array's 4th component
         }
         tc::fence_before_sync();
     }

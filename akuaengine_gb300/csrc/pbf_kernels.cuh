@@ -177,36 +177,44 @@ __global__ void __launch_bounds__(kElemBlock)
              const float4* __restrict__ dp_in, float* __restrict__ rho_out,
              float* __restrict__ lam_out, float4* __restrict__ dp_out, int carry,
              const float* __restrict__ lacc_src, float* __restrict__ lprev_out,
-             float* __restrict__ speed_out) {
+             float* __restrict__ speed_out, uint32_t* __restrict__ mass_bits) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= P->n) return;
-    const StepParams& p = params_for(P, s);
-    const uint32_t r = spr[s];
-    const uint32_t o = refperm[r];
-    const float4 x = x4[o];
-    const float4 v = v4[o];
-    const float3 xs = predict(p, x, v);
-    if (speed_out) {  // learned modes: |predicted velocity| and last step's accumulated lambda
-        const float vx = __fmaf_rn(p.gravity[0], p.dt, v.x);
-        const float vy = __fmaf_rn(p.gravity[1], p.dt, v.y);
-        const float vz = __fmaf_rn(p.gravity[2], p.dt, v.z);
-        speed_out[s] = sqrtf(vx * vx + vy * vy + vz * vz);
-        lprev_out[s] = lacc_src[o];
+    // masses: mass_bits[0] stays 0 while every mass has the bit pattern of record 0, which
+    // mass_bits[1] holds; a warp that sees another pattern sets mass_bits[0] once
+    const uint32_t ref_bits = __float_as_uint(__ldg(&x4[0].w));
+    bool other = false;
+    if (s < P->n) {
+        const StepParams& p = params_for(P, s);
+        const uint32_t r = spr[s];
+        const uint32_t o = refperm[r];
+        const float4 x = x4[o];
+        const float4 v = v4[o];
+        const float3 xs = predict(p, x, v);
+        if (speed_out) {  // learned modes: |predicted velocity| and last step's accumulated lambda
+            const float vx = __fmaf_rn(p.gravity[0], p.dt, v.x);
+            const float vy = __fmaf_rn(p.gravity[1], p.dt, v.y);
+            const float vz = __fmaf_rn(p.gravity[2], p.dt, v.z);
+            speed_out[s] = sqrtf(vx * vx + vy * vy + vz * vz);
+            lprev_out[s] = lacc_src[o];
+        }
+        const float4 q = make_float4(xs.x, xs.y, xs.z, x.w);
+        x4g[s] = x;
+        col4g[s] = col4[o];
+        sizeg[s] = size[o];
+        ps0[s] = q;
+        r2i[r] = (uint32_t)s;
+        rank_of[s] = r;
+        xref[r] = q;
+        order_out[r] = rref_old[o];
+        if (carry) {
+            rho_out[s] = rho_in[o];
+            lam_out[s] = lam_in[o];
+            dp_out[s] = dp_in[o];
+        }
+        other = __float_as_uint(x.w) != ref_bits;
+        if (s == 0) mass_bits[1] = ref_bits;
     }
-    const float4 q = make_float4(xs.x, xs.y, xs.z, x.w);
-    x4g[s] = x;
-    col4g[s] = col4[o];
-    sizeg[s] = size[o];
-    ps0[s] = q;
-    r2i[r] = (uint32_t)s;
-    rank_of[s] = r;
-    xref[r] = q;
-    order_out[r] = rref_old[o];
-    if (carry) {
-        rho_out[s] = rho_in[o];
-        lam_out[s] = lam_in[o];
-        dp_out[s] = dp_in[o];
-    }
+    if (__any_sync(0xFFFFFFFFu, other) && (threadIdx.x & 31) == 0) atomicOr(mass_bits, 1u);
 }
 
 // The bucket table (NeighbourSearchCUDA.cu:52-65 builds hash -> first sorted index).  Here an

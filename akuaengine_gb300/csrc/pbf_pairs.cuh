@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(128)
     k_density_lambda(const StepParams* __restrict__ P, const float4* __restrict__ ps,
                      const uint4* __restrict__ nbr4, const uint32_t* __restrict__ cnt,
                      float* __restrict__ rho_out, float* __restrict__ lam_out,
-                     float* __restrict__ lacc) {
+                     float* __restrict__ lacc, float4* __restrict__ psl) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P->n) return;
     const StepParams& p = params_for(P, i);
@@ -139,6 +139,7 @@ __global__ void __launch_bounds__(128)
     rho_out[i] = acc.rho;
     const float l = acc.lambda(p);
     lam_out[i] = l;
+    psl[i] = make_float4(xi.x, xi.y, xi.z, l);
     if (lacc) lacc[i] += l;  // learned modes: the step's accumulated lambda
 }
 
@@ -194,6 +195,50 @@ __device__ __forceinline__ float3 position_delta(const StepParams& p, int n, flo
     return make_float3(dx * p.inv_rho0, dy * p.inv_rho0, dz * p.inv_rho0);
 }
 
+// The same sum when every particle has mass `m`: positions and lambdas come from one 16-byte
+// gather of psl[j] = (x*_j, lambda_j), and (lambda_i + lambda_j + s_corr) * m is the same product.
+template <bool EXACT>
+__device__ __forceinline__ float3 position_delta_uniform(const StepParams& p, int n, float4 xl,
+                                                         const float4* __restrict__ psl, float m,
+                                                         const uint4* __restrict__ col, int c) {
+    float dx = 0.f, dy = 0.f, dz = 0.f;
+    for_each_pair(col, n, c, [&](uint32_t j0, uint32_t j1, bool two) {
+        const float4 a = __ldg(psl + j0), b = __ldg(psl + j1);
+        const float2 sx = sub2(f2(xl.x), make_float2(a.x, b.x));
+        const float2 sy = sub2(f2(xl.y), make_float2(a.y, b.y));
+        const float2 sz = sub2(f2(xl.z), make_float2(a.z, b.z));
+        const float2 r2 = len2_2(sx, sy, sz);
+        const float2 pw = scorr_pow2<EXACT>(p, r2);
+        const float2 bb = mul2(fma2(f2(p.neg_k), pw, add2(f2(xl.w), make_float2(a.w, b.w))), f2(m));
+        float2 gx, gy, gz;
+        spiky2<EXACT>(p, sx, sy, sz, r2, gx, gy, gz);
+        dx = __fmaf_rn(bb.x, gx.x, dx);
+        dy = __fmaf_rn(bb.x, gy.x, dy);
+        dz = __fmaf_rn(bb.x, gz.x, dz);
+        if (two) {
+            dx = __fmaf_rn(bb.y, gx.y, dx);
+            dy = __fmaf_rn(bb.y, gy.y, dy);
+            dz = __fmaf_rn(bb.y, gz.y, dz);
+        }
+    });
+    return make_float3(dx * p.inv_rho0, dy * p.inv_rho0, dz * p.inv_rho0);
+}
+
+// Delta of particle i: the single-gather form when the step's masses all have one bit pattern
+// (mass_bits = {0 when they do, that pattern}, from k_gather), else the general one.
+template <bool EXACT>
+__device__ __forceinline__ float3 delta_of(const StepParams& p, int i, float4 xi,
+                                           const float4* __restrict__ ps_in,
+                                           const float* __restrict__ lam,
+                                           const float4* __restrict__ psl,
+                                           const uint32_t* __restrict__ mass_bits,
+                                           const uint4* __restrict__ nbr4, int c) {
+    if (__ldg(mass_bits) == 0u)
+        return position_delta_uniform<EXACT>(p, p.n, psl[i], psl, __uint_as_float(__ldg(mass_bits + 1)),
+                                             nbr4 + i, c);
+    return position_delta<EXACT>(p, p.n, xi, lam[i], ps_in, lam, nbr4 + i, c);
+}
+
 // Soft box clamp of one coordinate (ConstraintSolverCUDA.cu:136-157).
 __device__ __forceinline__ float clamp_axis(float x, float lo_wall, float hi_wall) {
     const float lo = lo_wall + 0.025f, hi = hi_wall - 0.025f;
@@ -208,13 +253,14 @@ __global__ void __launch_bounds__(128)
     k_delta_correct(const StepParams* __restrict__ P, const float4* __restrict__ ps_in,
                     const float* __restrict__ lam, const uint4* __restrict__ nbr4,
                     const uint32_t* __restrict__ cnt, float4* __restrict__ ps_out,
-                    float4* __restrict__ dp4) {
+                    float4* __restrict__ dp4, const float4* __restrict__ psl,
+                    const uint32_t* __restrict__ mass_bits) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P->n) return;
     const StepParams& p = params_for(P, i);
     if (i >= p.n) return;
     const float4 xi = ps_in[i];
-    const float3 d = position_delta<EXACT>(p, p.n, xi, lam[i], ps_in, lam, nbr4 + i, (int)cnt[i]);
+    const float3 d = delta_of<EXACT>(p, i, xi, ps_in, lam, psl, mass_bits, nbr4, (int)cnt[i]);
     dp4[i] = make_float4(d.x, d.y, d.z, 0.f);
     ps_out[i] = make_float4(clamp_axis(xi.x + d.x, p.box_min[0], p.box_max[0]),
                             clamp_axis(xi.y + d.y, p.box_min[1], p.box_max[1]),
@@ -258,7 +304,8 @@ __global__ void __launch_bounds__(128)
                   float* __restrict__ size, const uint32_t* __restrict__ rref_new,
                   uint32_t* __restrict__ rref, const float* __restrict__ rho_c,
                   const float* __restrict__ lam_c, const float4* __restrict__ dp_c,
-                  float* __restrict__ rho, float* __restrict__ lam_out, int has_delta) {
+                  float* __restrict__ rho, float* __restrict__ lam_out, int has_delta,
+                  const float4* __restrict__ psl, const uint32_t* __restrict__ mass_bits) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P->n) return;
     const StepParams& p = params_for(P, i);
@@ -266,8 +313,7 @@ __global__ void __launch_bounds__(128)
     const float4 xi = ps_in[i];
     float nx = xi.x, ny = xi.y, nz = xi.z;
     if (has_delta) {
-        const float3 d =
-            position_delta<EXACT>(p, p.n, xi, lam[i], ps_in, lam, nbr4 + i, (int)cnt[i]);
+        const float3 d = delta_of<EXACT>(p, i, xi, ps_in, lam, psl, mass_bits, nbr4, (int)cnt[i]);
         dp4[i] = make_float4(d.x, d.y, d.z, 0.f);
         nx = clamp_axis(xi.x + d.x, p.box_min[0], p.box_max[0]);
         ny = clamp_axis(xi.y + d.y, p.box_min[1], p.box_max[1]);

@@ -52,7 +52,7 @@ __global__ void __launch_bounds__(kSearchBlock)
              uint32_t* __restrict__ cnt, float* __restrict__ rho_out, float* __restrict__ lam_out,
              uint32_t* __restrict__ flags, int density, const float* __restrict__ speed,
              const float* __restrict__ lprev, float* __restrict__ lacc,
-             float* __restrict__ feat) {
+             float* __restrict__ feat, float4* __restrict__ psl) {
     extern __shared__ __align__(16) uint32_t stage[];
     const StepParams& p = *P;
     const int n = p.n;
@@ -175,6 +175,7 @@ __global__ void __launch_bounds__(kSearchBlock)
         rho_out[i] = acc.rho;
         const float l = acc.lambda(p);
         lam_out[i] = l;
+        psl[i] = make_float4(xi.x, xi.y, xi.z, l);
         if (feat) {  // learned modes: the lambda sum starts; the network's features
             lacc[i] = l;
             write_features(params_for(P, i), acc, l, count, lprev[i], speed[i],

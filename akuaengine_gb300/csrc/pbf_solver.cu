@@ -64,6 +64,8 @@ struct akua_pbf {
     uint32_t* sort_scratch = nullptr;
     uint2* table = nullptr;
     uint32_t *nbr = nullptr, *cnt = nullptr, *flags = nullptr;
+    float4* psl = nullptr;          // (x*, lambda) of the current iteration, for uniform masses
+    uint32_t* mass_bits = nullptr;  // {another mass seen, record 0's mass bits} of this step
     char* staging = nullptr;
     size_t staging_bytes = 0;
 
@@ -113,7 +115,7 @@ struct akua_pbf {
 
 namespace akua::mlp {
 int enqueue_forward(const akua_mlp* m, const float* feat, int n, float* out, float* out2,
-                    cudaStream_t st);
+                    float* out4, cudaStream_t st);
 }
 
 namespace {
@@ -139,7 +141,7 @@ void free_all(akua_pbf* s) {
                     s->ka0, s->va0, s->ka1, s->va1, s->kb0, s->vb0, s->kb1, s->vb1,
                     s->sort_scratch, s->table, s->nbr, s->cnt, s->flags, s->staging,
                     s->feat, s->lacc, s->lprev, s->lacc_ref, s->speed, s->err_max, s->err_sum,
-                    s->scene_of};
+                    s->scene_of, s->psl, s->mass_bits};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (s->exec) cudaGraphExecDestroy(s->exec);
@@ -304,10 +306,11 @@ void enqueue_pairs(akua_pbf* s, cudaStream_t st, Marker& mark) {
     akua::k_search<EXACT><<<grid_for(n, akua::kSearchBlock), akua::kSearchBlock,
                             akua::kSearchSmem, st>>>(
         s->d_params, s->ps0, s->xref, s->table, s->r2i, s->nbr, s->cnt, s->rho, s->lam,
-        s->flags, iters > 0 ? 1 : 0, s->speed, s->lprev, s->lacc, learn ? s->feat : nullptr);
+        s->flags, iters > 0 ? 1 : 0, s->speed, s->lprev, s->lacc, learn ? s->feat : nullptr,
+        s->psl);
     mark("k_search");
     if (learn == 2) {
-        akua::mlp::enqueue_forward(s->warm, s->feat, n, s->lam, s->lacc, st);
+        akua::mlp::enqueue_forward(s->warm, s->feat, n, s->lam, s->lacc, &s->psl->w, st);
         mark("k_mlp_forward");
     }
     akua::k_table_clear<<<grid_for(n, akua::kElemBlock), akua::kElemBlock, 0, st>>>(s->d_params,
@@ -319,18 +322,18 @@ void enqueue_pairs(akua_pbf* s, cudaStream_t st, Marker& mark) {
         if (it > 0) {
             akua::k_density_lambda<EXACT><<<gp, akua::kPairBlock, 0, st>>>(
                 s->d_params, cur, nbr4, s->cnt, s->rho, s->lam,
-                learn == 1 ? s->lacc : nullptr);  // warm: the network's estimate is the sum
+                learn == 1 ? s->lacc : nullptr, s->psl);  // warm: the network's estimate is the sum
             mark("k_density_lambda");
         }
         if (it + 1 < iters) {
             akua::k_delta_correct<EXACT><<<gp, akua::kPairBlock, 0, st>>>(
-                s->d_params, cur, s->lam, nbr4, s->cnt, nxt, s->dp4);
+                s->d_params, cur, s->lam, nbr4, s->cnt, nxt, s->dp4, s->psl, s->mass_bits);
             mark("k_delta_correct");
         } else {
             akua::k_delta_final<EXACT><<<gp, akua::kPairBlock, 0, st>>>(
                 s->d_params, cur, s->lam, nbr4, s->cnt, s->x4g, s->x4, s->v4, s->vstar4, s->dp4,
                 s->col4g, s->sizeg, s->col4, s->size, s->rrefg, s->rref, s->rhog, s->lamg, s->dpg,
-                s->rho, s->lam, 1);
+                s->rho, s->lam, 1, s->psl, s->mass_bits);
             mark("k_delta_final");
         }
     }
@@ -338,7 +341,7 @@ void enqueue_pairs(akua_pbf* s, cudaStream_t st, Marker& mark) {
         akua::k_delta_final<EXACT><<<gp, akua::kPairBlock, 0, st>>>(
             s->d_params, s->ps0, s->lam, nbr4, s->cnt, s->x4g, s->x4, s->v4, s->vstar4, s->dp4,
             s->col4g, s->sizeg, s->col4, s->size, s->rrefg, s->rref, s->rhog, s->lamg, s->dpg,
-            s->rho, s->lam, 0);
+            s->rho, s->lam, 0, s->psl, s->mass_bits);
         mark("k_delta_final");
     }
     akua::k_vorticity<EXACT><<<gp, akua::kPairBlock, 0, st>>>(s->d_params, s->x4, s->v4, nbr4,
@@ -369,11 +372,12 @@ void enqueue_body(akua_pbf* s, cudaStream_t st, const char* aos, size_t stride, 
     mark("k_morton_ref");
     akua::radix::sort_pairs(st, s->plan_sp, s->kb0, s->vb0, s->kb1, s->vb1, true, s->sort_scratch,
                             n, &dummy, &s->spperm, mark);
+    cudaMemsetAsync(s->mass_bits, 0, sizeof(uint32_t), st);  // "another mass seen" flag
     akua::k_gather<<<ge, akua::kElemBlock, 0, st>>>(
         s->d_params, s->spperm, s->refperm, s->x4, s->v4, s->col4, s->size, s->rref, s->x4g,
         s->col4g, s->sizeg, s->ps0, s->r2i, s->rrefg, s->xref, s->order, s->rho, s->lam, s->dp4,
         s->rhog, s->lamg, s->dpg, carry ? 1 : 0, s->lacc, s->lprev,
-        learn_mode(s) ? s->speed : nullptr);
+        learn_mode(s) ? s->speed : nullptr, s->mass_bits);
     mark("k_gather");
     akua::k_ref_table<<<ge, akua::kElemBlock, 0, st>>>(s->d_params, s->kr, s->table, s->bmix);
     mark("k_ref_table");
@@ -607,6 +611,8 @@ int create_solver(int32_t n, const akua_pbf_config* cfg, const akua_lambda_corr_
     chk(dalloc(s, &s->nbr, N * 4 * ((cap + 3) / 4)));  // uint4 tiles of 4 entries
     chk(dalloc(s, &s->cnt, N));
     chk(dalloc(s, &s->flags, 1));
+    chk(dalloc(s, &s->psl, N));
+    chk(dalloc(s, &s->mass_bits, 2));
     if (e == cudaSuccess) e = cudaMemset(s->table, 0, sizeof(uint2) * (size_t)s->table_alloc);
     if (e == cudaSuccess) e = cudaMemset(s->flags, 0, sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemset(s->dp4, 0, sizeof(float4) * N);

@@ -141,6 +141,24 @@ def test_long_lists_bitexact(cap, table_size):
     assert_records_bitexact(g, o)
 
 
+@pytest.mark.parametrize("masses", ["uniform_0.7", "varied"])
+def test_masses_bitexact(masses):
+    """The Jacobi delta gathers (x*, lambda) in one load when every mass has the same bit
+    pattern, and positions, masses and lambdas separately otherwise: both bit-exact."""
+    sc = scene.workload("dam_break_27k", seed=8)
+    p = sc.particles.copy()
+    if masses == "varied":
+        p["mass"] = np.random.default_rng(1).uniform(0.8, 1.2, sc.n).astype(np.float32)
+    else:
+        p["mass"] = np.float32(0.7)
+    cfg, corr = bench_params()
+    cfg.restDensity = float(np.float32(7600.0 * float(p["mass"].mean())))
+    g, ge = run_gpu(sc, cfg, corr, 3, ak.OPT_EXACT_MATH, particles=p)
+    o, oe = run_oracle(sc, cfg, corr, 3, particles=p)
+    assert_grid_equal(ge, oe, cfg.maxNeighbours)
+    assert_records_bitexact(g, o)
+
+
 def test_small_table_collisions_bitexact():
     """A 4096-entry table makes many cells share a bucket (duplicated and foreign candidates)."""
     sc = scene.dam_break((12, 12, 12), (3.0, 3.0, 3.0), seed=4)
