@@ -91,6 +91,14 @@ class CCamera(ctypes.Structure):
                 ("nearZ", ctypes.c_float), ("farZ", ctypes.c_float)]
 
 
+class CSdfShape(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_int32), ("a", ctypes.c_float * 3), ("b", ctypes.c_float * 3),
+                ("radius", ctypes.c_float)]
+
+
+SDF_SPHERE, SDF_BOX, SDF_CAPSULE, SDF_PLANE = 1, 2, 3, 4
+
+
 class CStats(ctypes.Structure):
     _fields_ = [
         ("numParticles", ctypes.c_int32),
@@ -154,6 +162,8 @@ _SIGS = {
                                             ctypes.POINTER(ctypes.c_int32)]),
     "akua_sort_pairs_noalloc": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int32, ctypes.c_int32, _P]),
     "akua_pbf_set_solver_iterations": (ctypes.c_int, [_P, ctypes.c_int32]),
+    "akua_pbf_set_sdf_shapes": (ctypes.c_int, [_P, ctypes.POINTER(CSdfShape), ctypes.c_int32,
+                                               ctypes.c_float, ctypes.c_float]),
     "akua_camera_default": (None, [ctypes.POINTER(CCamera)]),
     "akua_camera_matrices": (ctypes.c_int, [ctypes.POINTER(CCamera), ctypes.c_float, _P, _P, _P]),
     "akua_splat_create": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(_P)]),

@@ -16,6 +16,19 @@ namespace akua {
 // Everything a kernel of one step reads besides the particle arrays.  Lives in device memory and is
 // rewritten by a one-thread kernel at the start of every step, so a captured step graph replays
 // with new dt / box / gravity without re-capture.
+// Solid obstacles as signed distance functions (SDF boundary; the reference's clamp is a stand-in
+// for a boundary of this kind, ConstraintSolverCUDA.cu:131-134).  type: 1 sphere (centre a,
+// radius), 2 axis-aligned box (centre a, half extents b, corner radius), 3 capsule (segment a-b,
+// radius), 4 half-space (unit normal a pointing into the fluid, offset b[0]: solid where
+// a . x < b[0]).
+struct SdfShape {
+    int32_t type;
+    float a[3];
+    float b[3];
+    float radius;
+};
+enum { kSdfSphere = 1, kSdfBox = 2, kSdfCapsule = 3, kSdfPlane = 4 };
+
 struct StepParams {
     // PBFConfig-derived constants
     float h;            // smoothRadius
@@ -56,6 +69,11 @@ struct StepParams {
     int32_t scene;
     uint32_t table_offset;
     const uint16_t* scene_of;
+    // SDF obstacles (none: the reference's box clamp alone)
+    const SdfShape* shapes;
+    int32_t num_shapes;
+    float sdf_min_dist;
+    float sdf_stiffness;
 };
 
 // The parameters of the scene particle (or reference rank, or internal slot) i belongs to.
@@ -98,6 +116,66 @@ __device__ __forceinline__ uint32_t cell_hash(int cx, int cy, int cz, uint32_t t
     const uint32_t hy = static_cast<uint32_t>(cy) * 19349663u;
     const uint32_t hz = static_cast<uint32_t>(cz) * 83492791u;
     return fast_mod(hx ^ hy ^ hz, magic, table);
+}
+
+// Signed distance from the solid of shape s (positive on the fluid side) and its unit gradient,
+// in plain IEEE single operations (no contraction); the host restatement uses the same ones.
+__device__ __forceinline__ float sdf_eval(const SdfShape& s, float x, float y, float z, float* n) {
+    if (s.type == kSdfPlane) {
+        n[0] = s.a[0]; n[1] = s.a[1]; n[2] = s.a[2];
+        return (s.a[0] * x + s.a[1] * y + s.a[2] * z) - s.b[0];
+    }
+    float dx, dy, dz;
+    if (s.type == kSdfBox) {
+        const float px = x - s.a[0], py = y - s.a[1], pz = z - s.a[2];
+        const float qx = fabsf(px) - s.b[0], qy = fabsf(py) - s.b[1], qz = fabsf(pz) - s.b[2];
+        const float ox = fmaxf(qx, 0.f), oy = fmaxf(qy, 0.f), oz = fmaxf(qz, 0.f);
+        const float lo = __fsqrt_rn(ox * ox + oy * oy + oz * oz);
+        const float qm = fmaxf(qx, fmaxf(qy, qz));
+        if (lo > 0.f) {
+            n[0] = __fdiv_rn(copysignf(ox, px), lo);
+            n[1] = __fdiv_rn(copysignf(oy, py), lo);
+            n[2] = __fdiv_rn(copysignf(oz, pz), lo);
+        } else {  // inside: out through the nearest face (x before y before z on ties)
+            n[0] = n[1] = n[2] = 0.f;
+            const int k = (qx == qm) ? 0 : ((qy == qm) ? 1 : 2);
+            const float pk = k == 0 ? px : (k == 1 ? py : pz);
+            n[k] = pk < 0.f ? -1.f : 1.f;
+        }
+        return (lo + fminf(qm, 0.f)) - s.radius;
+    }
+    if (s.type == kSdfCapsule) {
+        const float ux = s.b[0] - s.a[0], uy = s.b[1] - s.a[1], uz = s.b[2] - s.a[2];
+        const float wx = x - s.a[0], wy = y - s.a[1], wz = z - s.a[2];
+        const float uu = ux * ux + uy * uy + uz * uz;
+        float t = uu > 0.f ? __fdiv_rn(wx * ux + wy * uy + wz * uz, uu) : 0.f;
+        t = fminf(fmaxf(t, 0.f), 1.f);
+        dx = wx - t * ux; dy = wy - t * uy; dz = wz - t * uz;
+    } else {  // sphere
+        dx = x - s.a[0]; dy = y - s.a[1]; dz = z - s.a[2];
+    }
+    const float l = __fsqrt_rn(dx * dx + dy * dy + dz * dz);
+    if (l > 0.f) {
+        n[0] = __fdiv_rn(dx, l); n[1] = __fdiv_rn(dy, l); n[2] = __fdiv_rn(dz, l);
+    } else {
+        n[0] = 0.f; n[1] = 1.f; n[2] = 0.f;
+    }
+    return l - s.radius;
+}
+
+// Pushes a corrected position out of every obstacle it comes within sdf_min_dist of (soft, like
+// the box clamp): x += stiffness * (min_dist - phi) * grad phi, shapes in order.
+__device__ __forceinline__ void sdf_correct(const StepParams& p, float& x, float& y, float& z) {
+    for (int k = 0; k < p.num_shapes; ++k) {
+        float n[3];
+        const float phi = sdf_eval(p.shapes[k], x, y, z, n);
+        if (phi < p.sdf_min_dist) {
+            const float c = p.sdf_stiffness * (p.sdf_min_dist - phi);
+            x = x + c * n[0];
+            y = y + c * n[1];
+            z = z + c * n[2];
+        }
+    }
 }
 
 // poly6 (SmoothingKernelsCUDA.h:16-21): 0 when r2 > h2, else kp * (h2 - r2)^3.

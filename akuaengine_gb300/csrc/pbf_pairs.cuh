@@ -262,9 +262,11 @@ __global__ void __launch_bounds__(128)
     const float4 xi = ps_in[i];
     const float3 d = delta_of<EXACT>(p, i, xi, ps_in, lam, psl, mass_bits, nbr4, (int)cnt[i]);
     dp4[i] = make_float4(d.x, d.y, d.z, 0.f);
-    ps_out[i] = make_float4(clamp_axis(xi.x + d.x, p.box_min[0], p.box_max[0]),
-                            clamp_axis(xi.y + d.y, p.box_min[1], p.box_max[1]),
-                            clamp_axis(xi.z + d.z, p.box_min[2], p.box_max[2]), xi.w);
+    float nx = clamp_axis(xi.x + d.x, p.box_min[0], p.box_max[0]);
+    float ny = clamp_axis(xi.y + d.y, p.box_min[1], p.box_max[1]);
+    float nz = clamp_axis(xi.z + d.z, p.box_min[2], p.box_max[2]);
+    sdf_correct(p, nx, ny, nz);
+    ps_out[i] = make_float4(nx, ny, nz, xi.w);
 }
 
 // resolve_collision against one axis-aligned plane (IntegrationCUDA.cu:51-73), with the plane
@@ -318,6 +320,7 @@ __global__ void __launch_bounds__(128)
         nx = clamp_axis(xi.x + d.x, p.box_min[0], p.box_max[0]);
         ny = clamp_axis(xi.y + d.y, p.box_min[1], p.box_max[1]);
         nz = clamp_axis(xi.z + d.z, p.box_min[2], p.box_max[2]);
+        sdf_correct(p, nx, ny, nz);
     } else {
         rho[i] = rho_c[i];
         lam_out[i] = lam_c[i];
@@ -335,6 +338,25 @@ __global__ void __launch_bounds__(128)
     damp_plane(p, nx, ny, nz, 0.f, p.box_max[1], 0.f, 0.f, -1.f, 0.f, vx, vy, vz);
     damp_plane(p, nx, ny, nz, 0.f, 0.f, p.box_min[2], 0.f, 0.f, 1.f, vx, vy, vz);
     damp_plane(p, nx, ny, nz, 0.f, 0.f, p.box_max[2], 0.f, 0.f, -1.f, vx, vy, vz);
+    // the same damping against each obstacle, along its SDF gradient (plain dot products)
+    for (int k = 0; k < p.num_shapes; ++k) {
+        float g[3];
+        const float dist = sdf_eval(p.shapes[k], nx, ny, nz, g);
+        const float appr = vx * g[0] + vy * g[1] + vz * g[2];
+        if (dist < p.sdf_min_dist) {
+            const float vnx = appr * g[0], vny = appr * g[1], vnz = appr * g[2];
+            const float tx = vx - vnx, ty = vy - vny, tz = vz - vnz;
+            if (appr < 0.0f) {
+                vx = __fmaf_rn(p.neg_restitution, vnx, p.keep * tx);
+                vy = __fmaf_rn(p.neg_restitution, vny, p.keep * ty);
+                vz = __fmaf_rn(p.neg_restitution, vnz, p.keep * tz);
+            } else if (fabsf(appr) < 1e-5f) {
+                vx = p.keep * tx;
+                vy = p.keep * ty;
+                vz = p.keep * tz;
+            }
+        }
+    }
     x4[i] = make_float4(nx, ny, nz, xi.w);
     v4[i] = make_float4(vx, vy, vz, 0.f);
     col4[i] = col4g[i];

@@ -65,6 +65,9 @@ struct akua_pbf {
     uint2* table = nullptr;
     uint32_t *nbr = nullptr, *cnt = nullptr, *flags = nullptr;
     float4* psl = nullptr;          // (x*, lambda) of the current iteration, for uniform masses
+    akua::SdfShape* shapes = nullptr;  // SDF obstacles (device), AKUA_SDF_MAX_SHAPES
+    int num_shapes = 0;
+    float sdf_min_dist = 0.025f, sdf_stiffness = 0.5f;
     uint32_t* mass_bits = nullptr;  // {another mass seen, record 0's mass bits} of this step
     char* staging = nullptr;
     size_t staging_bytes = 0;
@@ -141,7 +144,7 @@ void free_all(akua_pbf* s) {
                     s->ka0, s->va0, s->ka1, s->va1, s->kb0, s->vb0, s->kb1, s->vb1,
                     s->sort_scratch, s->table, s->nbr, s->cnt, s->flags, s->staging,
                     s->feat, s->lacc, s->lprev, s->lacc_ref, s->speed, s->err_max, s->err_sum,
-                    s->scene_of, s->psl, s->mass_bits};
+                    s->scene_of, s->psl, s->mass_bits, s->shapes};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (s->exec) cudaGraphExecDestroy(s->exec);
@@ -224,6 +227,10 @@ StepParams make_params(const akua_pbf* s, float dt, const float* bmin, const flo
     p.table_size = s->table_size;
     p.table_magic = UINT64_MAX / (uint64_t)s->table_size + 1u;
     p.sp_bits = morton_bits(s, bmin, bmax, p.sp_origin);
+    p.shapes = s->shapes;
+    p.num_shapes = s->num_shapes;
+    p.sdf_min_dist = s->sdf_min_dist;
+    p.sdf_stiffness = s->sdf_stiffness;
     return p;
 }
 
@@ -612,6 +619,7 @@ int create_solver(int32_t n, const akua_pbf_config* cfg, const akua_lambda_corr_
     chk(dalloc(s, &s->cnt, N));
     chk(dalloc(s, &s->flags, 1));
     chk(dalloc(s, &s->psl, N));
+    chk(dalloc(s, &s->shapes, AKUA_SDF_MAX_SHAPES));
     chk(dalloc(s, &s->mass_bits, 2));
     if (e == cudaSuccess) e = cudaMemset(s->table, 0, sizeof(uint2) * (size_t)s->table_alloc);
     if (e == cudaSuccess) e = cudaMemset(s->flags, 0, sizeof(uint32_t));
@@ -1004,6 +1012,30 @@ int akua_pbf_set_lambda_tracking(akua_pbf* s, int32_t enabled) {
         if (e != cudaSuccess) return cuda_status(e);
     }
     s->track = enabled != 0;
+    return AKUA_OK;
+}
+
+int akua_pbf_set_sdf_shapes(akua_pbf* s, const akua_sdf_shape* shapes, int32_t count,
+                            float minDist, float stiffness) {
+    if (!s || count < 0 || count > AKUA_SDF_MAX_SHAPES || (count > 0 && !shapes) ||
+        !std::isfinite(minDist) || !std::isfinite(stiffness))
+        return AKUA_ERR_INVALID_ARGUMENT;
+    static_assert(sizeof(akua_sdf_shape) == sizeof(akua::SdfShape), "shape layout");
+    for (int k = 0; k < count; ++k) {
+        const akua_sdf_shape& d = shapes[k];
+        if (d.type < AKUA_SDF_SPHERE || d.type > AKUA_SDF_PLANE || !finite3(d.a) || !finite3(d.b) ||
+            !std::isfinite(d.radius))
+            return AKUA_ERR_INVALID_ARGUMENT;
+    }
+    DeviceGuard g(s->device);
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e == cudaSuccess && count > 0)
+        e = cudaMemcpy(s->shapes, shapes, sizeof(akua_sdf_shape) * (size_t)count,
+                       cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_status(e);
+    s->num_shapes = count;
+    s->sdf_min_dist = minDist;
+    s->sdf_stiffness = stiffness;
     return AKUA_OK;
 }
 

@@ -169,6 +169,15 @@ class PBFSolver:
               "akua_pbf_capture_training")
         self._capture = (features, targets)
 
+    def set_sdf_shapes(self, shapes, min_dist: float = 0.025, stiffness: float = 0.5) -> None:
+        """Solid obstacles: dicts with type ("sphere", "box", "capsule", "plane" or the
+        AKUA_SDF_* number), a, b, radius (see include/akua_pbf.h).  [] removes them."""
+        arr = (_abi.CSdfShape * max(len(shapes), 1))()
+        for k, d in enumerate(shapes):
+            arr[k] = sdf_shape(d)
+        check(self._lib.akua_pbf_set_sdf_shapes(self._h, arr, len(shapes), float(min_dist),
+                                                float(stiffness)), "akua_pbf_set_sdf_shapes")
+
     def set_lambda_tracking(self, enabled: bool) -> None:
         check(self._lib.akua_pbf_set_lambda_tracking(self._h, int(bool(enabled))),
               "akua_pbf_set_lambda_tracking")
@@ -311,4 +320,19 @@ def _scene_desc(d) -> "_abi.CSceneDesc":
         c.gravity[a] = float(_get(d, "gravity")[a])
         c.boxMin[a] = float(_get(d, "box_min")[a])
         c.boxMax[a] = float(_get(d, "box_max")[a])
+    return c
+
+
+SDF_TYPES = {"sphere": _abi.SDF_SPHERE, "box": _abi.SDF_BOX, "capsule": _abi.SDF_CAPSULE,
+             "plane": _abi.SDF_PLANE}
+
+
+def sdf_shape(d) -> "_abi.CSdfShape":
+    c = _abi.CSdfShape()
+    t = d["type"]
+    c.type = SDF_TYPES[t] if isinstance(t, str) else int(t)
+    for q in range(3):
+        c.a[q] = float(d.get("a", (0.0, 0.0, 0.0))[q])
+        c.b[q] = float(d.get("b", (0.0, 0.0, 0.0))[q])
+    c.radius = float(d.get("radius", 0.0))
     return c

@@ -212,6 +212,26 @@ int akua_pbf_step_batch(akua_pbf* solver, float deltaTime);
 /* Changes scene `scene`'s gravity and box (numParticles must stay the same). */
 int akua_pbf_set_scene(akua_pbf* solver, int32_t scene, const akua_scene_desc* desc);
 
+/* ---- SDF obstacles.  The reference clamps particles to the box and plans a proper boundary in its
+ * place (ConstraintSolverCUDA.cu:131-134); here solid shapes given by signed distance functions
+ * are added to the box: after each Jacobi correction (and the box clamp) a particle within
+ * minDist of an obstacle moves by stiffness * (minDist - phi) along the SDF gradient (the box
+ * clamp's rule, 0.025 and 0.5 there), and the update damps the velocity against each obstacle as
+ * against the box's planes.  No shapes (the default): the reference's step exactly. */
+#define AKUA_SDF_SPHERE 1   /* a = centre, radius */
+#define AKUA_SDF_BOX 2      /* a = centre, b = half extents, radius = corner rounding */
+#define AKUA_SDF_CAPSULE 3  /* segment a-b, radius */
+#define AKUA_SDF_PLANE 4    /* a = unit normal into the fluid, b[0] = offset: solid where a.x < b[0] */
+#define AKUA_SDF_MAX_SHAPES 64
+typedef struct akua_sdf_shape {
+    int32_t type;
+    float a[3];
+    float b[3];
+    float radius;
+} akua_sdf_shape;
+int akua_pbf_set_sdf_shapes(akua_pbf* solver, const akua_sdf_shape* shapes, int32_t count,
+                            float minDist, float stiffness);
+
 /* ---- State files.  No counterpart in the reference (its scene is rebuilt in code each run). ----
  * A file holds the particle records of a simulation and what resuming it needs: the solver
  * parameters, box, time step, step count and table size, optionally the per-particle lambda sums

@@ -48,7 +48,35 @@ class OracleParams(ctypes.Structure):
         ("friction", ctypes.c_float),
         ("flags", ctypes.c_uint32),
         ("num_threads", ctypes.c_int32),
+        ("num_shapes", ctypes.c_int32),
+        ("sdf_min_dist", ctypes.c_float),
+        ("sdf_stiffness", ctypes.c_float),
+        ("pad_", ctypes.c_int32),
+        ("shapes", ctypes.c_void_p),
     ]
+
+
+class OracleShape(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_int32), ("a", ctypes.c_float * 3), ("b", ctypes.c_float * 3),
+                ("radius", ctypes.c_float)]
+
+
+def set_shapes(P: "OracleParams", shapes, min_dist: float = 0.025, stiffness: float = 0.5):
+    """Attaches SDF obstacles (dicts with type, a, b, radius) to oracle parameters; the array is
+    kept alive on P."""
+    arr = (OracleShape * max(len(shapes), 1))()
+    for k, d in enumerate(shapes):
+        arr[k].type = int(d["type"])
+        for q in range(3):
+            arr[k].a[q] = float(d.get("a", (0, 0, 0))[q])
+            arr[k].b[q] = float(d.get("b", (0, 0, 0))[q])
+        arr[k].radius = float(d.get("radius", 0.0))
+    P.num_shapes = len(shapes)
+    P.sdf_min_dist = float(min_dist)
+    P.sdf_stiffness = float(stiffness)
+    P.shapes = ctypes.cast(arr, ctypes.c_void_p)
+    P._shape_array = arr
+    return P
 
 
 def build(force: bool = False) -> str:

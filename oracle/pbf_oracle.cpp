@@ -18,6 +18,9 @@
 //   XSPH               src/CUDA/IntegrationCUDA.cu:167-195 (read from a velocity snapshot; the
 //                      reference reads neighbours' velocities while other threads overwrite them)
 //   poly6 / spiky      include/AkuaEngine/CUDA/SmoothingKernelsCUDA.h:16-28 (pi written as 3.14f)
+//   SDF obstacles      not in the reference (it plans a boundary in place of its clamp,
+//                      ConstraintSolverCUDA.cu:131-134): applied after the box clamp and after
+//                      the six-plane damping, in plain single operations
 //   cross              include/AkuaEngine/CUDA/MathUtilsCUDA.h:12-18
 //
 // Arithmetic.  Every product-sum that the CUDA compiler contracts by default in the reference
@@ -81,6 +84,18 @@ struct OracleParams {
     float friction;           // 0.95 at the reference call site
     uint32_t flags;
     int32_t num_threads;      // <= 0: OpenMP default
+    int32_t num_shapes;       // SDF obstacles (0: none)
+    float sdf_min_dist;
+    float sdf_stiffness;
+    int32_t pad_;
+    const struct OracleShape* shapes;
+};
+
+struct OracleShape {  // type 1 sphere, 2 box, 3 capsule, 4 half-space (see sdf_eval)
+    int32_t type;
+    float a[3];
+    float b[3];
+    float radius;
 };
 
 enum { ORACLE_FMA = 1u, ORACLE_FP64 = 2u };
@@ -196,6 +211,53 @@ struct Grid {
     std::vector<uint32_t> nbr;  // n * cap, row-major (reference layout i*cap + k)
     std::vector<uint32_t> cnt;
 };
+
+// Signed distance from an obstacle (positive in the fluid) and its unit gradient.
+template <class R>
+R sdf_eval(const OracleShape& s, R x, R y, R z, R* n) {
+    const R a0 = s.a[0], a1 = s.a[1], a2 = s.a[2];
+    if (s.type == 4) {
+        n[0] = a0; n[1] = a1; n[2] = a2;
+        return (a0 * x + a1 * y + a2 * z) - (R)s.b[0];
+    }
+    R dx, dy, dz;
+    if (s.type == 2) {
+        const R px = x - a0, py = y - a1, pz = z - a2;
+        const R qx = std::fabs(px) - (R)s.b[0], qy = std::fabs(py) - (R)s.b[1],
+                qz = std::fabs(pz) - (R)s.b[2];
+        const R ox = std::fmax(qx, R(0)), oy = std::fmax(qy, R(0)), oz = std::fmax(qz, R(0));
+        const R lo = std::sqrt(ox * ox + oy * oy + oz * oz);
+        const R qm = std::fmax(qx, std::fmax(qy, qz));
+        if (lo > R(0)) {
+            n[0] = std::copysign(ox, px) / lo;
+            n[1] = std::copysign(oy, py) / lo;
+            n[2] = std::copysign(oz, pz) / lo;
+        } else {
+            n[0] = n[1] = n[2] = R(0);
+            const int k = (qx == qm) ? 0 : ((qy == qm) ? 1 : 2);
+            const R pk = k == 0 ? px : (k == 1 ? py : pz);
+            n[k] = pk < R(0) ? R(-1) : R(1);
+        }
+        return (lo + std::fmin(qm, R(0))) - (R)s.radius;
+    }
+    if (s.type == 3) {
+        const R ux = (R)s.b[0] - a0, uy = (R)s.b[1] - a1, uz = (R)s.b[2] - a2;
+        const R wx = x - a0, wy = y - a1, wz = z - a2;
+        const R uu = ux * ux + uy * uy + uz * uz;
+        R t = uu > R(0) ? (wx * ux + wy * uy + wz * uz) / uu : R(0);
+        t = std::fmin(std::fmax(t, R(0)), R(1));
+        dx = wx - t * ux; dy = wy - t * uy; dz = wz - t * uz;
+    } else {
+        dx = x - a0; dy = y - a1; dz = z - a2;
+    }
+    const R l = std::sqrt(dx * dx + dy * dy + dz * dz);
+    if (l > R(0)) {
+        n[0] = dx / l; n[1] = dy / l; n[2] = dz / l;
+    } else {
+        n[0] = R(0); n[1] = R(1); n[2] = R(0);
+    }
+    return l - (R)s.radius;
+}
 
 template <bool FMA>
 void neighbour_search(const OracleParams& P, int n, const std::vector<ParticleRec>& ps, Grid& g) {
@@ -370,6 +432,14 @@ int step_impl(const OracleParams& P, int n, ParticleRec* particles, uint32_t* ou
                 if (pc[a] > hi) c = fmac<FMA>(stiff, hi - pc[a], c);
                 pc[a] = pc[a] + c;
             }
+            for (int k = 0; k < P.num_shapes; ++k) {  // SDF obstacles
+                R g[3];
+                const R phi = sdf_eval<R>(P.shapes[k], p.x, p.y, p.z, g);
+                if (phi < (R)P.sdf_min_dist) {
+                    const R c = (R)P.sdf_stiffness * ((R)P.sdf_min_dist - phi);
+                    p = {p.x + c * g[0], p.y + c * g[1], p.z + c * g[2]};
+                }
+            }
             xs_next[i] = p;
         }
         std::swap(xs, xs_next);
@@ -398,6 +468,21 @@ int step_impl(const OracleParams& P, int n, ParticleRec* particles, uint32_t* ou
             const R appr = dot3<FMA>(vel, nrm[q]);
             if (dist < md) {
                 const V3<R> vn{appr * nrm[q].x, appr * nrm[q].y, appr * nrm[q].z};
+                const V3<R> vt = sub(vel, vn);
+                if (appr < R(0)) {
+                    vel = {fmac<FMA>(-rest, vn.x, keep * vt.x), fmac<FMA>(-rest, vn.y, keep * vt.y),
+                           fmac<FMA>(-rest, vn.z, keep * vt.z)};
+                } else if (std::fabs(appr) < (R)1e-5f) {
+                    vel = {keep * vt.x, keep * vt.y, keep * vt.z};
+                }
+            }
+        }
+        for (int k = 0; k < P.num_shapes; ++k) {  // SDF obstacles, plain dot products
+            R g[3];
+            const R dist = sdf_eval<R>(P.shapes[k], x[i].x, x[i].y, x[i].z, g);
+            const R appr = vel.x * g[0] + vel.y * g[1] + vel.z * g[2];
+            if (dist < (R)P.sdf_min_dist) {
+                const V3<R> vn{appr * g[0], appr * g[1], appr * g[2]};
                 const V3<R> vt = sub(vel, vn);
                 if (appr < R(0)) {
                     vel = {fmac<FMA>(-rest, vn.x, keep * vt.x), fmac<FMA>(-rest, vn.y, keep * vt.y),
