@@ -51,6 +51,22 @@ enum RecWord : int {
     kMass = 18, kDensity = 19, kLambda = 20, kHash = 21, kColor = 22, kSize = 26, kRecWords = 27
 };
 
+// Block-wide copy of `words` floats, in 16-byte pieces when both ends allow it (a block of
+// kIoBlock packed 108-byte records starts on a 16-byte boundary of a 16-byte aligned array); the
+// records may live in host memory read over the host link, where wide accesses matter most.
+__device__ __forceinline__ void copy_words(float* __restrict__ dst, const float* __restrict__ src,
+                                           int words) {
+    int done = 0;
+    if ((((uintptr_t)dst | (uintptr_t)src) & 15u) == 0) {
+        const int vec = words >> 2;
+        const uint4* s4 = reinterpret_cast<const uint4*>(src);
+        uint4* d4 = reinterpret_cast<uint4*>(dst);
+        for (int w = threadIdx.x; w < vec; w += blockDim.x) d4[w] = s4[w];
+        done = vec << 2;
+    }
+    for (int w = done + threadIdx.x; w < words; w += blockDim.x) dst[w] = src[w];
+}
+
 __global__ void k_set_params(StepParams p, StepParams* __restrict__ dst) {
     if (threadIdx.x == 0 && blockIdx.x == 0) *dst = p;
 }
@@ -75,12 +91,12 @@ __global__ void __launch_bounds__(kIoBlock)
              float4* __restrict__ v4, float4* __restrict__ col4, float* __restrict__ size,
              uint32_t* __restrict__ rref, float* __restrict__ rho, float* __restrict__ lam,
              float4* __restrict__ dp4, int carry) {
-    __shared__ float rec[kIoBlock * kRecWords];
+    __shared__ __align__(16) float rec[kIoBlock * kRecWords];
     const int r0 = blockIdx.x * kIoBlock;
     const int cnt = min(kIoBlock, n - r0);
     if (stride == kRecWords * 4) {
         const float* src = reinterpret_cast<const float*>(aos) + (size_t)r0 * kRecWords;
-        for (int w = threadIdx.x; w < cnt * kRecWords; w += kIoBlock) rec[w] = src[w];
+        copy_words(rec, src, cnt * kRecWords);
     } else {
         for (int w = threadIdx.x; w < cnt * kRecWords; w += kIoBlock) {
             const int q = w / kRecWords, f = w - q * kRecWords;
@@ -290,7 +306,7 @@ __global__ void __launch_bounds__(kIoBlock)
              const float* __restrict__ rho, const float* __restrict__ lam,
              const float4* __restrict__ col4, const float* __restrict__ size,
              const float* __restrict__ lacc, float* __restrict__ lacc_ref) {
-    __shared__ float rec[kIoBlock * kRecWords];
+    __shared__ __align__(16) float rec[kIoBlock * kRecWords];
     const int r0 = blockIdx.x * kIoBlock;
     const int cnt = min(kIoBlock, n - r0);
     const int t = threadIdx.x;
@@ -316,7 +332,7 @@ __global__ void __launch_bounds__(kIoBlock)
     __syncthreads();
     if (stride == kRecWords * 4) {
         float* dst = reinterpret_cast<float*>(aos) + (size_t)r0 * kRecWords;
-        for (int w = t; w < cnt * kRecWords; w += kIoBlock) dst[w] = rec[w];
+        copy_words(dst, rec, cnt * kRecWords);
     } else {
         for (int w = t; w < cnt * kRecWords; w += kIoBlock) {
             const int q = w / kRecWords, f = w - q * kRecWords;

@@ -719,6 +719,17 @@ int akua_pbf_step_host(akua_pbf* s, void* host, size_t stride, float dt, const f
     if (!s || !host || stride < sizeof(akua_particle) || stride % 4 != 0 || !s->scenes.empty())
         return AKUA_ERR_INVALID_ARGUMENT;
     DeviceGuard g(s->device);
+    // Pinned records: the import and export kernels read and write them in place over the host
+    // link, with no staging copies.  Other host memory goes through a device staging buffer.
+    cudaPointerAttributes attr{};
+    if (cudaPointerGetAttributes(&attr, host) == cudaSuccess && attr.type == cudaMemoryTypeHost &&
+        attr.devicePointer) {
+        const int rc = do_step(s, static_cast<const char*>(attr.devicePointer), stride, true, dt,
+                               bmin, bmax);
+        if (rc != AKUA_OK) return rc;
+        return cuda_status(cudaStreamSynchronize(s->stream));
+    }
+    cudaGetLastError();
     const size_t bytes = (size_t)s->n * stride;
     if (s->staging_bytes < bytes) {
         if (s->staging) {

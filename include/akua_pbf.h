@@ -123,9 +123,10 @@ int akua_pbf_attach_particles(akua_pbf* solver, void* deviceParticles, size_t st
  * XSPH viscosity over the attached buffer.  Asynchronous on the handle's stream. */
 int akua_pbf_step(akua_pbf* solver, float deltaTime, const float boxMin[3], const float boxMax[3]);
 
-/* The same step for callers that hold the particle array in host memory: copies the N records
- * to the device, steps, and copies them back (stride as in akua_pbf_attach_particles).
- * Synchronous: returns after the records are back in `hostParticles`. */
+/* The same step for callers that hold the particle array in host memory (stride as in
+ * akua_pbf_attach_particles).  Pinned memory (cudaHostAlloc, cudaHostRegister) is read and
+ * written in place by the step's import and export kernels; other memory is copied to a device
+ * buffer and back.  Synchronous: returns after the records are back in `hostParticles`. */
 int akua_pbf_step_host(akua_pbf* solver, void* hostParticles, size_t strideBytes, float deltaTime,
                        const float boxMin[3], const float boxMax[3]);
 

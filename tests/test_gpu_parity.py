@@ -328,6 +328,24 @@ def test_fast_error_against_fp64_oracle():
 
 # --- host logic of the step: graph, resident state, device buffers ---------------------------
 
+def test_step_host_pinned_and_pageable_identical():
+    """Pinned host records are stepped in place over the host link; pageable ones through a
+    device copy: same bytes, over several steps."""
+    import torch
+
+    sc = scene.workload("dam_break_27k", seed=12)
+    cfg, corr = bench_params()
+    pinned = torch.empty(sc.particles.nbytes, dtype=torch.uint8, pin_memory=True)
+    pinned.numpy()[:] = sc.particles.view(np.uint8)
+    pv = pinned.numpy().view(ak.PARTICLE_DTYPE)
+    pageable = sc.particles.copy()
+    with PBFSolver(sc.n, cfg, corr) as a, PBFSolver(sc.n, cfg, corr) as b:
+        for _ in range(4):
+            a.step_host(pv, sc.dt, sc.box_min, sc.box_max)
+            b.step_host(pageable, sc.dt, sc.box_min, sc.box_max)
+    assert pv.tobytes() == pageable.tobytes()
+
+
 def test_graph_and_direct_launch_identical():
     sc = scene.dam_break((16, 16, 16), (3.0, 3.0, 3.0), seed=11)
     cfg, corr = bench_params()
