@@ -7,7 +7,10 @@
 //     follow it.
 //   * the internal order: particles sorted by the Morton code of their cell, so that a warp's
 //     particles and their neighbours sit close together in memory.  All per-particle state and the
-//     neighbour passes use it.
+//     neighbour passes use it.  It is a stable sort over the previous reference order, so it does
+//     not wait for the hash sort: particles of one cell share their hash, so their order within
+//     the cell is their new reference order either way (cells that share a clamped Morton key
+//     and are not contiguous are found by k_bucket_meta and walked by rank).
 // Results do not depend on the internal order: every per-particle sum runs over the neighbour list
 // in the reference's walk order.
 //
@@ -15,7 +18,7 @@
 //   predict              IntegrationCUDA.cu:27-36            k_keys, k_gather
 //   cell hash            NeighbourSearchCUDA.cu:15-44        k_keys
 //   sort by hash         NeighbourSearchCUDA.cu:167-170      radix sort of (hash, previous rank)
-//   bucket starts        NeighbourSearchCUDA.cu:52-65        k_ref, k_bucket_len
+//   bucket starts        NeighbourSearchCUDA.cu:52-65        k_ref_table, k_bucket_meta, k_table_fill
 //   neighbour walk       NeighbourSearchCUDA.cu:72-130       k_search (+ iteration 1 density/lambda)
 //   density, lambda      ConstraintSolverCUDA.cu:16-97       k_search / k_density_lambda
 //   delta, correct       ConstraintSolverCUDA.cu:99-169      k_delta_correct / k_delta_final
@@ -147,12 +150,14 @@ __device__ __forceinline__ uint32_t morton_key(const StepParams& p, int cx, int 
     return spread10(x) | (spread10(y) << 1) | (spread10(z) << 2);
 }
 
-// Cell hash of the predicted position, scattered into the previous reference order so the stable
-// sort ties like the reference's; and the Morton key of the walk cell, by current internal index.
+// Cell hash and Morton key of the walk cell of each predicted position, both scattered into the
+// previous reference order (so both stable sorts tie like the reference's), each with the import
+// index as payload.
 __global__ void __launch_bounds__(kElemBlock)
     k_keys(const StepParams* __restrict__ P, const float4* __restrict__ x4,
            const float4* __restrict__ v4, const uint32_t* __restrict__ rref,
-           uint32_t* __restrict__ akey, uint32_t* __restrict__ aval, uint32_t* __restrict__ mkey) {
+           uint32_t* __restrict__ akey, uint32_t* __restrict__ aval, uint32_t* __restrict__ bkey,
+           uint32_t* __restrict__ bval) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P->n) return;
     const StepParams& p = params_for(P, i);
@@ -162,28 +167,29 @@ __global__ void __launch_bounds__(kElemBlock)
     const uint32_t r = rref[i];
     akey[r] = p.table_offset + h;
     aval[r] = (uint32_t)i;
-    mkey[i] = ((uint32_t)p.scene << (3 * p.sp_bits)) |
+    bkey[r] = ((uint32_t)p.scene << (3 * p.sp_bits)) |
               morton_key(p, cell_coord(xs.x, p.search_cell), cell_coord(xs.y, p.search_cell),
                          cell_coord(xs.z, p.search_cell));
+    bval[r] = (uint32_t)i;
 }
 
-// Morton keys laid out in the new reference order.  Sorting them stably keeps the particles of one
-// cell in reference-rank order inside the internal order, so a bucket that holds a single cell is
-// a contiguous run of internal slots.
+// The new reference rank of every particle, by import index (the inverse of the hash sort's
+// permutation), for the gather.
 __global__ void __launch_bounds__(kElemBlock)
-    k_morton_ref(const StepParams* __restrict__ P, const uint32_t* __restrict__ refperm,
-                 const uint32_t* __restrict__ mkey, uint32_t* __restrict__ skey) {
+    k_rank_scatter(const StepParams* __restrict__ P, const uint32_t* __restrict__ refperm,
+                   uint32_t* __restrict__ rank_of_import) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= P->n) return;
-    skey[r] = mkey[refperm[r]];
+    rank_of_import[refperm[r]] = (uint32_t)r;
 }
 
-// Moves the state into the new internal order (slot s holds the particle of reference rank
-// spr[s]) and writes the predicted positions, both maps between ranks and slots, the
-// reference-ordered predicted positions and the debug order (pre-sort record index per rank).
+// Moves the state into the new internal order (slot s holds the particle of import index
+// sp_import[s], reference rank rank_of_import[...]) and writes the predicted positions, both maps
+// between ranks and slots, the reference-ordered predicted positions and the debug order
+// (pre-sort record index per rank).
 __global__ void __launch_bounds__(kElemBlock)
-    k_gather(const StepParams* __restrict__ P, const uint32_t* __restrict__ spr,
-             const uint32_t* __restrict__ refperm, const float4* __restrict__ x4,
+    k_gather(const StepParams* __restrict__ P, const uint32_t* __restrict__ sp_import,
+             const uint32_t* __restrict__ rank_of_import, const float4* __restrict__ x4,
              const float4* __restrict__ v4, const float4* __restrict__ col4,
              const float* __restrict__ size, const uint32_t* __restrict__ rref_old,
              float4* __restrict__ x4g, float4* __restrict__ col4g, float* __restrict__ sizeg,
@@ -201,8 +207,8 @@ __global__ void __launch_bounds__(kElemBlock)
     bool other = false;
     if (s < P->n) {
         const StepParams& p = params_for(P, s);
-        const uint32_t r = spr[s];
-        const uint32_t o = refperm[r];
+        const uint32_t o = sp_import[s];       // import index of internal slot s
+        const uint32_t r = rank_of_import[o];  // its new reference rank
         const float4 x = x4[o];
         const float4 v = v4[o];
         const float3 xs = predict(p, x, v);

@@ -56,12 +56,15 @@ struct akua_pbf {
     float4 *x4g = nullptr, *col4g = nullptr, *ps0 = nullptr, *ps1 = nullptr;
     float4 *vstar4 = nullptr, *om4 = nullptr, *vc4 = nullptr, *dpg = nullptr, *xref = nullptr;
     float *sizeg = nullptr, *rhog = nullptr, *lamg = nullptr;
-    uint32_t *rrefg = nullptr, *mkey = nullptr, *r2i = nullptr, *blen = nullptr, *order = nullptr;
+    uint32_t *rrefg = nullptr, *rank_of_import = nullptr, *r2i = nullptr, *blen = nullptr, *order = nullptr;
     uint32_t* bmix = nullptr;  // per bucket start: nonzero when the bucket is not one internal run
     // sorts: reference order (A) and Morton order (B)
     uint32_t *ka0 = nullptr, *va0 = nullptr, *ka1 = nullptr, *va1 = nullptr;
     uint32_t *kb0 = nullptr, *vb0 = nullptr, *kb1 = nullptr, *vb1 = nullptr;
     uint32_t* sort_scratch = nullptr;
+    uint32_t* sort_scratch_b = nullptr;  // the Morton sort's, which runs beside the hash sort
+    cudaStream_t side_stream = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     uint2* table = nullptr;
     uint32_t *nbr = nullptr, *cnt = nullptr, *flags = nullptr;
     float4* psl = nullptr;          // (x*, lambda) of the current iteration, for uniform masses
@@ -140,9 +143,10 @@ cudaError_t dalloc(akua_pbf* s, T** p, size_t count) {
 void free_all(akua_pbf* s) {
     void* ptrs[] = {s->d_params, s->x4, s->v4, s->col4, s->size, s->rref, s->rho, s->lam, s->dp4,
                     s->x4g, s->col4g, s->ps0, s->ps1, s->vstar4, s->om4, s->vc4, s->dpg, s->xref,
-                    s->sizeg, s->rhog, s->lamg, s->rrefg, s->mkey, s->r2i, s->blen, s->order, s->bmix,
+                    s->sizeg, s->rhog, s->lamg, s->rrefg, s->rank_of_import, s->r2i, s->blen, s->order, s->bmix,
                     s->ka0, s->va0, s->ka1, s->va1, s->kb0, s->vb0, s->kb1, s->vb1,
-                    s->sort_scratch, s->table, s->nbr, s->cnt, s->flags, s->staging,
+                    s->sort_scratch, s->sort_scratch_b, s->table, s->nbr, s->cnt, s->flags,
+                    s->staging,
                     s->feat, s->lacc, s->lprev, s->lacc_ref, s->speed, s->err_max, s->err_sum,
                     s->scene_of, s->psl, s->mass_bits, s->shapes};
     for (void* p : ptrs)
@@ -150,6 +154,9 @@ void free_all(akua_pbf* s) {
     if (s->exec) cudaGraphExecDestroy(s->exec);
     if (s->graph) cudaGraphDestroy(s->graph);
     if (s->capture_stream) cudaStreamDestroy(s->capture_stream);
+    if (s->side_stream) cudaStreamDestroy(s->side_stream);
+    if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+    if (s->ev_join) cudaEventDestroy(s->ev_join);
     for (cudaEvent_t ev : s->prof_events) cudaEventDestroy(ev);
 }
 
@@ -368,20 +375,35 @@ void enqueue_body(akua_pbf* s, cudaStream_t st, const char* aos, size_t stride, 
     Marker mark{s, st, record};
     const bool carry = s->cfg.solverIterations == 0;
     akua::k_keys<<<ge, akua::kElemBlock, 0, st>>>(s->d_params, s->x4, s->v4, s->rref, s->ka0,
-                                                  s->va0, s->mkey);
+                                                  s->va0, s->kb0, s->vb0);
     mark("k_keys");
     uint32_t* dummy = nullptr;
-    // reference order: stable by (hash, previous reference rank)
+    // The two sorts are independent: reference order, stable by (hash, previous reference rank),
+    // and internal order, stable by Morton cell over the previous reference order (payload: import
+    // index).  Outside profiling the second runs on a side stream, a parallel branch of the graph.
+    const bool fork = !record;
+    cudaStream_t sb = st;
+    Marker mark_b{s, st, record};
+    if (fork) {
+        cudaEventRecord(s->ev_fork, st);
+        cudaStreamWaitEvent(s->side_stream, s->ev_fork, 0);
+        sb = s->side_stream;
+        mark_b = Marker{s, sb, false};
+    }
+    akua::radix::sort_pairs(sb, s->plan_sp, s->kb0, s->vb0, s->kb1, s->vb1, false,
+                            s->sort_scratch_b, n, &dummy, &s->spperm, fork ? mark_b : mark);
+    if (fork) cudaEventRecord(s->ev_join, sb);
     akua::radix::sort_pairs(st, s->plan_ref, s->ka0, s->va0, s->ka1, s->va1, false,
                             s->sort_scratch, n, &s->kr, &s->refperm, mark);
-    // internal order: stable by Morton cell over the new reference order; payload = rank
-    akua::k_morton_ref<<<ge, akua::kElemBlock, 0, st>>>(s->d_params, s->refperm, s->mkey, s->kb0);
-    mark("k_morton_ref");
-    akua::radix::sort_pairs(st, s->plan_sp, s->kb0, s->vb0, s->kb1, s->vb1, true, s->sort_scratch,
-                            n, &dummy, &s->spperm, mark);
+    akua::k_rank_scatter<<<ge, akua::kElemBlock, 0, st>>>(s->d_params, s->refperm, s->rank_of_import);
+    mark("k_rank_scatter");
+    if (fork) {
+        cudaStreamWaitEvent(st, s->ev_join, 0);
+        mark.launches += mark_b.launches;
+    }
     cudaMemsetAsync(s->mass_bits, 0, sizeof(uint32_t), st);  // "another mass seen" flag
     akua::k_gather<<<ge, akua::kElemBlock, 0, st>>>(
-        s->d_params, s->spperm, s->refperm, s->x4, s->v4, s->col4, s->size, s->rref, s->x4g,
+        s->d_params, s->spperm, s->rank_of_import, s->x4, s->v4, s->col4, s->size, s->rref, s->x4g,
         s->col4g, s->sizeg, s->ps0, s->r2i, s->rrefg, s->xref, s->order, s->rho, s->lam, s->dp4,
         s->rhog, s->lamg, s->dpg, carry ? 1 : 0, s->lacc, s->lprev,
         learn_mode(s) ? s->speed : nullptr, s->mass_bits);
@@ -606,7 +628,7 @@ int create_solver(int32_t n, const akua_pbf_config* cfg, const akua_lambda_corr_
     chk(dalloc(s, &s->vstar4, N)); chk(dalloc(s, &s->om4, N)); chk(dalloc(s, &s->vc4, N));
     chk(dalloc(s, &s->dpg, N)); chk(dalloc(s, &s->xref, N));
     chk(dalloc(s, &s->sizeg, N)); chk(dalloc(s, &s->rhog, N)); chk(dalloc(s, &s->lamg, N));
-    chk(dalloc(s, &s->rrefg, N)); chk(dalloc(s, &s->mkey, N)); chk(dalloc(s, &s->r2i, N));
+    chk(dalloc(s, &s->rrefg, N)); chk(dalloc(s, &s->rank_of_import, N)); chk(dalloc(s, &s->r2i, N));
     chk(dalloc(s, &s->bmix, N));
     chk(dalloc(s, &s->blen, N)); chk(dalloc(s, &s->order, N));
     chk(dalloc(s, &s->ka0, N)); chk(dalloc(s, &s->va0, N));
@@ -614,6 +636,7 @@ int create_solver(int32_t n, const akua_pbf_config* cfg, const akua_lambda_corr_
     chk(dalloc(s, &s->kb0, N)); chk(dalloc(s, &s->vb0, N));
     chk(dalloc(s, &s->kb1, N)); chk(dalloc(s, &s->vb1, N));
     chk(dalloc(s, &s->sort_scratch, akua::radix::scratch_words(n)));
+    chk(dalloc(s, &s->sort_scratch_b, akua::radix::scratch_words(n)));
     chk(dalloc(s, &s->table, (size_t)s->table_alloc));
     chk(dalloc(s, &s->nbr, N * 4 * ((cap + 3) / 4)));  // uint4 tiles of 4 entries
     chk(dalloc(s, &s->cnt, N));
@@ -625,6 +648,9 @@ int create_solver(int32_t n, const akua_pbf_config* cfg, const akua_lambda_corr_
     if (e == cudaSuccess) e = cudaMemset(s->flags, 0, sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemset(s->dp4, 0, sizeof(float4) * N);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->capture_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->side_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming);
     // the staged neighbour walk needs more than the default 48 KB of dynamic shared memory
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(akua::k_search<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
