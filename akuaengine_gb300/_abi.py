@@ -162,6 +162,10 @@ _SIGS = {
                                             ctypes.POINTER(ctypes.c_int32)]),
     "akua_sort_pairs_noalloc": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int32, ctypes.c_int32, _P]),
     "akua_pbf_set_solver_iterations": (ctypes.c_int, [_P, ctypes.c_int32]),
+    "akua_pbf_set_pair_blocks": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int32)]),
+    "akua_pbf_get_pair_blocks": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int32)]),
+    "akua_pbf_autotune": (ctypes.c_int, [_P, ctypes.c_float, _P, _P, ctypes.c_int32,
+                                         ctypes.POINTER(ctypes.c_int32)]),
     "akua_pbf_set_sdf_shapes": (ctypes.c_int, [_P, ctypes.POINTER(CSdfShape), ctypes.c_int32,
                                                ctypes.c_float, ctypes.c_float]),
     "akua_camera_default": (None, [ctypes.POINTER(CCamera)]),

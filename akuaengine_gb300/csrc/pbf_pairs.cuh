@@ -16,6 +16,10 @@
 
 namespace akua {
 
+// The neighbour-pair kernels run with a block size chosen per kernel (64, 128 or 256 threads; the
+// solver's autotuner picks them by measurement); results do not depend on it.
+constexpr int kMaxPairBlock = 256;
+
 __device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 // a - b: fma(b, -1, a) is the exact difference rounded once, i.e. the IEEE subtraction.
@@ -120,7 +124,7 @@ struct DensityLambda2 {
 };
 
 template <bool EXACT>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(kMaxPairBlock)
     k_density_lambda(const StepParams* __restrict__ P, const float4* __restrict__ ps,
                      const uint4* __restrict__ nbr4, const uint32_t* __restrict__ cnt,
                      float* __restrict__ rho_out, float* __restrict__ lam_out,
@@ -249,7 +253,7 @@ __device__ __forceinline__ float clamp_axis(float x, float lo_wall, float hi_wal
 }
 
 template <bool EXACT>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(kMaxPairBlock)
     k_delta_correct(const StepParams* __restrict__ P, const float4* __restrict__ ps_in,
                     const float* __restrict__ lam, const uint4* __restrict__ nbr4,
                     const uint32_t* __restrict__ cnt, float4* __restrict__ ps_out,
@@ -296,7 +300,7 @@ __device__ __forceinline__ void damp_plane(const StepParams& p, float px, float 
 // go straight to the update and the carried density/lambda/delta move into the state.  Also moves
 // the gathered colour, size and reference rank into the state arrays.
 template <bool EXACT>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(kMaxPairBlock)
     k_delta_final(const StepParams* __restrict__ P, const float4* __restrict__ ps_in,
                   const float* __restrict__ lam, const uint4* __restrict__ nbr4,
                   const uint32_t* __restrict__ cnt, const float4* __restrict__ x_old,
@@ -367,7 +371,7 @@ __global__ void __launch_bounds__(128)
 // omega_i = sum_j -m_j (v_j - v_i) x grad W(x_i - x_j)  (IntegrationCUDA.cu:104-128).
 // om4.w = |omega_i| for the confinement pass.
 template <bool EXACT>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(kMaxPairBlock)
     k_vorticity(const StepParams* __restrict__ P, const float4* __restrict__ x4,
                 const float4* __restrict__ v4, const uint4* __restrict__ nbr4,
                 const uint32_t* __restrict__ cnt, float4* __restrict__ om4) {
@@ -408,7 +412,7 @@ __global__ void __launch_bounds__(128)
 // Vorticity confinement (IntegrationCUDA.cu:130-165); writes the confined velocity to a separate
 // buffer with vc4.w = m_i / rho_i for the XSPH pass.
 template <bool EXACT>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(kMaxPairBlock)
     k_confine(const StepParams* __restrict__ P, const float4* __restrict__ x4,
               const float4* __restrict__ v4, const float4* __restrict__ om4,
               const float* __restrict__ rho, const uint4* __restrict__ nbr4,
@@ -462,7 +466,7 @@ __global__ void __launch_bounds__(128)
 }
 
 // XSPH viscosity (IntegrationCUDA.cu:167-195) from the confined-velocity snapshot vc4.
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(kMaxPairBlock)
     k_xsph(const StepParams* __restrict__ P, const float4* __restrict__ x4,
            const float4* __restrict__ vc4, const uint4* __restrict__ nbr4,
            const uint32_t* __restrict__ cnt, float4* __restrict__ v4) {

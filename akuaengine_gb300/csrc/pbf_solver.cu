@@ -108,6 +108,9 @@ struct akua_pbf {
     uint16_t* scene_of = nullptr;       // device: the scene of every particle
     int scene_bits = 0;                 // bits of the scene index in the Morton sort key
 
+    // block sizes of the neighbour-pair kernels (akua_pbf_set_pair_blocks / akua_pbf_autotune)
+    int pair_block[AKUA_PBF_PAIR_KERNELS] = {128, 128, 128, 128, 128, 128};
+
     int64_t steps = 0;
     uint64_t device_bytes = 0;
 
@@ -312,7 +315,8 @@ struct Marker {
 template <bool EXACT>
 void enqueue_pairs(akua_pbf* s, cudaStream_t st, Marker& mark) {
     const int n = s->n;
-    const int gp = grid_for(n, akua::kPairBlock);
+    const int* pb = s->pair_block;  // per kernel: density, delta, last delta, vort., conf., XSPH
+    auto gp = [&](int k) { return grid_for(n, pb[k]); };
     const int iters = s->cfg.solverIterations;
     float4* ps[2] = {s->ps0, s->ps1};
     const uint4* nbr4 = reinterpret_cast<const uint4*>(s->nbr);
@@ -334,17 +338,17 @@ void enqueue_pairs(akua_pbf* s, cudaStream_t st, Marker& mark) {
         float4* cur = ps[it & 1];
         float4* nxt = ps[(it + 1) & 1];
         if (it > 0) {
-            akua::k_density_lambda<EXACT><<<gp, akua::kPairBlock, 0, st>>>(
+            akua::k_density_lambda<EXACT><<<gp(0), pb[0], 0, st>>>(
                 s->d_params, cur, nbr4, s->cnt, s->rho, s->lam,
                 learn == 1 ? s->lacc : nullptr, s->psl);  // warm: the network's estimate is the sum
             mark("k_density_lambda");
         }
         if (it + 1 < iters) {
-            akua::k_delta_correct<EXACT><<<gp, akua::kPairBlock, 0, st>>>(
+            akua::k_delta_correct<EXACT><<<gp(1), pb[1], 0, st>>>(
                 s->d_params, cur, s->lam, nbr4, s->cnt, nxt, s->dp4, s->psl, s->mass_bits);
             mark("k_delta_correct");
         } else {
-            akua::k_delta_final<EXACT><<<gp, akua::kPairBlock, 0, st>>>(
+            akua::k_delta_final<EXACT><<<gp(2), pb[2], 0, st>>>(
                 s->d_params, cur, s->lam, nbr4, s->cnt, s->x4g, s->x4, s->v4, s->vstar4, s->dp4,
                 s->col4g, s->sizeg, s->col4, s->size, s->rrefg, s->rref, s->rhog, s->lamg, s->dpg,
                 s->rho, s->lam, 1, s->psl, s->mass_bits);
@@ -352,19 +356,19 @@ void enqueue_pairs(akua_pbf* s, cudaStream_t st, Marker& mark) {
         }
     }
     if (iters == 0) {
-        akua::k_delta_final<EXACT><<<gp, akua::kPairBlock, 0, st>>>(
+        akua::k_delta_final<EXACT><<<gp(2), pb[2], 0, st>>>(
             s->d_params, s->ps0, s->lam, nbr4, s->cnt, s->x4g, s->x4, s->v4, s->vstar4, s->dp4,
             s->col4g, s->sizeg, s->col4, s->size, s->rrefg, s->rref, s->rhog, s->lamg, s->dpg,
             s->rho, s->lam, 0, s->psl, s->mass_bits);
         mark("k_delta_final");
     }
-    akua::k_vorticity<EXACT><<<gp, akua::kPairBlock, 0, st>>>(s->d_params, s->x4, s->v4, nbr4,
+    akua::k_vorticity<EXACT><<<gp(3), pb[3], 0, st>>>(s->d_params, s->x4, s->v4, nbr4,
                                                               s->cnt, s->om4);
     mark("k_vorticity");
-    akua::k_confine<EXACT><<<gp, akua::kPairBlock, 0, st>>>(s->d_params, s->x4, s->v4, s->om4,
+    akua::k_confine<EXACT><<<gp(4), pb[4], 0, st>>>(s->d_params, s->x4, s->v4, s->om4,
                                                             s->rho, nbr4, s->cnt, s->vc4);
     mark("k_confine");
-    akua::k_xsph<<<gp, akua::kPairBlock, 0, st>>>(s->d_params, s->x4, s->vc4, nbr4, s->cnt, s->v4);
+    akua::k_xsph<<<gp(5), pb[5], 0, st>>>(s->d_params, s->x4, s->vc4, nbr4, s->cnt, s->v4);
     mark("k_xsph");
 }
 
@@ -1050,6 +1054,97 @@ int akua_pbf_set_lambda_tracking(akua_pbf* s, int32_t enabled) {
     }
     s->track = enabled != 0;
     return AKUA_OK;
+}
+
+int akua_pbf_set_pair_blocks(akua_pbf* s, const int32_t blocks[AKUA_PBF_PAIR_KERNELS]) {
+    if (!s || !blocks) return AKUA_ERR_INVALID_ARGUMENT;
+    for (int k = 0; k < AKUA_PBF_PAIR_KERNELS; ++k)
+        if (blocks[k] != 64 && blocks[k] != 128 && blocks[k] != 256)
+            return AKUA_ERR_INVALID_ARGUMENT;
+    for (int k = 0; k < AKUA_PBF_PAIR_KERNELS; ++k) s->pair_block[k] = blocks[k];
+    invalidate_graph(s);
+    return AKUA_OK;
+}
+
+int akua_pbf_get_pair_blocks(akua_pbf* s, int32_t blocks[AKUA_PBF_PAIR_KERNELS]) {
+    if (!s || !blocks) return AKUA_ERR_INVALID_ARGUMENT;
+    for (int k = 0; k < AKUA_PBF_PAIR_KERNELS; ++k) blocks[k] = s->pair_block[k];
+    return AKUA_OK;
+}
+
+int akua_pbf_autotune(akua_pbf* s, float dt, const float bmin[3], const float bmax[3],
+                      int32_t steps, int32_t* blocks_out) {
+    if (!s || steps <= 0 || steps > 100) return AKUA_ERR_INVALID_ARGUMENT;
+    if (!s->attached) return AKUA_ERR_NOT_ATTACHED;
+    DeviceGuard g(s->device);
+    static const char* const names[AKUA_PBF_PAIR_KERNELS] = {
+        "k_density_lambda", "k_delta_correct", "k_delta_final", "k_vorticity", "k_confine",
+        "k_xsph"};
+    const int cands[3] = {64, 128, 256};
+    const size_t bytes = (size_t)s->n * s->stride;
+    char* const user = s->attached;
+    const int64_t steps0 = s->steps;
+    float* const cap_f = s->cap_feat;
+    float* const cap_t = s->cap_target;
+    s->cap_feat = s->cap_target = nullptr;
+    char* tmp = nullptr;
+    float* sums = nullptr;
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&tmp), bytes);
+    if (e == cudaSuccess && s->lacc_ref)
+        e = cudaMalloc(reinterpret_cast<void**>(&sums), sizeof(float) * (size_t)s->n);
+    if (e == cudaSuccess && sums)
+        e = cudaMemcpy(sums, s->lacc_ref, sizeof(float) * (size_t)s->n, cudaMemcpyDeviceToDevice);
+    int rc = cuda_status(e);
+    double best[AKUA_PBF_PAIR_KERNELS];
+    int choice[AKUA_PBF_PAIR_KERNELS];
+    for (int k = 0; k < AKUA_PBF_PAIR_KERNELS; ++k) {
+        best[k] = 1e30;
+        choice[k] = s->pair_block[k];
+    }
+    std::vector<akua_kernel_time> times(64);
+    for (int c = 0; c < 3 && rc == AKUA_OK; ++c) {
+        for (int k = 0; k < AKUA_PBF_PAIR_KERNELS; ++k) s->pair_block[k] = cands[c];
+        invalidate_graph(s);
+        // every candidate starts from the same records (and lambda sums)
+        e = cudaMemcpy(tmp, user, bytes, cudaMemcpyDeviceToDevice);
+        if (e == cudaSuccess && sums)
+            e = cudaMemcpy(s->lacc_ref, sums, sizeof(float) * (size_t)s->n,
+                           cudaMemcpyDeviceToDevice);
+        rc = cuda_status(e);
+        if (rc == AKUA_OK) rc = do_step(s, tmp, s->stride, true, dt, bmin, bmax);
+        if (rc == AKUA_OK) rc = akua_pbf_profile_begin(s, steps);
+        for (int k = 0; k < steps && rc == AKUA_OK; ++k)
+            rc = do_step(s, tmp, s->stride, false, dt, bmin, bmax);
+        int32_t count = 0;
+        const int rc_end = akua_pbf_profile_end(s, times.data(), (int32_t)times.size(), &count);
+        if (rc == AKUA_OK) rc = rc_end;
+        for (int t = 0; t < count && rc == AKUA_OK; ++t)
+            for (int k = 0; k < AKUA_PBF_PAIR_KERNELS; ++k)
+                if (std::strcmp(times[t].name, names[k]) == 0 && times[t].launches > 0) {
+                    const double per = times[t].total_ms / times[t].launches;
+                    if (per < best[k]) {
+                        best[k] = per;
+                        choice[k] = cands[c];
+                    }
+                }
+    }
+    for (int k = 0; k < AKUA_PBF_PAIR_KERNELS; ++k) {
+        s->pair_block[k] = choice[k];
+        if (blocks_out) blocks_out[k] = choice[k];
+    }
+    invalidate_graph(s);
+    if (sums) {
+        cudaMemcpy(s->lacc_ref, sums, sizeof(float) * (size_t)s->n, cudaMemcpyDeviceToDevice);
+        cudaFree(sums);
+    }
+    if (tmp) cudaFree(tmp);
+    s->attached = user;
+    s->steps = steps0;
+    s->state_valid = false;  // the next step imports the user's records again
+    s->cap_feat = cap_f;
+    s->cap_target = cap_t;
+    return rc;
 }
 
 int akua_pbf_set_sdf_shapes(akua_pbf* s, const akua_sdf_shape* shapes, int32_t count,

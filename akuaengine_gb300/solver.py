@@ -169,6 +169,31 @@ class PBFSolver:
               "akua_pbf_capture_training")
         self._capture = (features, targets)
 
+    PAIR_KERNELS = ("k_density_lambda", "k_delta_correct", "k_delta_final", "k_vorticity",
+                    "k_confine", "k_xsph")
+
+    def pair_blocks(self) -> dict:
+        b = (ctypes.c_int32 * 6)()
+        check(self._lib.akua_pbf_get_pair_blocks(self._h, b), "akua_pbf_get_pair_blocks")
+        return dict(zip(self.PAIR_KERNELS, list(b)))
+
+    def set_pair_blocks(self, blocks) -> None:
+        """`blocks`: six block sizes (64, 128 or 256) or a dict by kernel name."""
+        if isinstance(blocks, dict):
+            blocks = [blocks[k] for k in self.PAIR_KERNELS]
+        b = (ctypes.c_int32 * 6)(*[int(x) for x in blocks])
+        check(self._lib.akua_pbf_set_pair_blocks(self._h, b), "akua_pbf_set_pair_blocks")
+
+    def autotune(self, deltaTime: float, boxMin=None, boxMax=None, steps: int = 3) -> dict:
+        """Chooses each pair kernel's block size by timing, on a copy of the attached records
+        (attach a buffer first); returns the choice by kernel name."""
+        b = (ctypes.c_int32 * 6)()
+        check(self._lib.akua_pbf_autotune(self._h, float(deltaTime),
+                                          None if boxMin is None else vec3(boxMin),
+                                          None if boxMax is None else vec3(boxMax), int(steps), b),
+              "akua_pbf_autotune")
+        return dict(zip(self.PAIR_KERNELS, list(b)))
+
     def set_sdf_shapes(self, shapes, min_dist: float = 0.025, stiffness: float = 0.5) -> None:
         """Solid obstacles: dicts with type ("sphere", "box", "capsule", "plane" or the
         AKUA_SDF_* number), a, b, radius (see include/akua_pbf.h).  [] removes them."""

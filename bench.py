@@ -318,6 +318,10 @@ def run_batched(args, cfg, corr):
     solver = BatchSolver(b.scenes, cfg, corr, stream=stream)
     buf = torch.from_numpy(b.particles.view(np.uint8).copy()).cuda()
     torch.cuda.synchronize()
+    from akuaengine_gb300.solver import as_particle_buffer
+
+    solver.attach(as_particle_buffer(buf))
+    pair_blocks = solver.autotune(b.dt, steps=3)
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             solver.step(buf, b.dt)
@@ -347,7 +351,8 @@ def run_batched(args, cfg, corr):
                        "scene_particles": [int(min(d["numParticles"] for d in b.scenes)),
                                            int(max(d["numParticles"] for d in b.scenes))],
                        "dt": b.dt, "solver_iterations": cfg.solverIterations,
-                       "table_size": int(cfg.maxNeighbours * b.n)},
+                       "table_size": int(cfg.maxNeighbours * b.n),
+                       "pair_blocks_autotuned": pair_blocks},
             "batch_step_ms": {"p50": round(float(np.percentile(per, 50)), 4),
                               "p99": round(float(np.percentile(per, 99)), 4),
                               "max": round(float(per.max()), 4)},
@@ -371,6 +376,7 @@ def run_ours(args, sc, cfg, corr):
 
     import akuaengine_gb300 as ak
     from akuaengine_gb300 import PBFSolver, replicas
+    from akuaengine_gb300.solver import as_particle_buffer
 
     world, rank, local = dist_env()
     torch.cuda.set_device(local)
@@ -387,6 +393,9 @@ def run_ours(args, sc, cfg, corr):
     host = sc.particles
     buf = torch.from_numpy(host.view(np.uint8).copy()).cuda()
     torch.cuda.synchronize()
+    # launch shapes of the pair kernels, chosen by the solver's autotuner on a copy of the records
+    solver.attach(as_particle_buffer(buf))
+    pair_blocks = solver.autotune(sc.dt, sc.box_min, sc.box_max, steps=3)
 
     def barrier():
         if dist is not None:
@@ -500,6 +509,7 @@ def run_ours(args, sc, cfg, corr):
                        "l2": "per-step working set > L2 (no flush)",
                        "mean_neighbours": round(mean_c, 3),
                        "list_bytes_per_particle": round(list_bytes, 2),
+                       "pair_blocks_autotuned": pair_blocks,
                        "buckets_per_particle": round(buckets_per_particle, 4)},
             "roofline": roofline,
             "cpu_baseline": cpu,

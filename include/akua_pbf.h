@@ -213,6 +213,21 @@ int akua_pbf_step_batch(akua_pbf* solver, float deltaTime);
 /* Changes scene `scene`'s gravity and box (numParticles must stay the same). */
 int akua_pbf_set_scene(akua_pbf* solver, int32_t scene, const akua_scene_desc* desc);
 
+/* ---- Launch shapes.  No counterpart in the reference (fixed 256-thread blocks). ---------------
+ * The neighbour-pair kernels (in this order: density and lambda, delta with correction, last
+ * delta with update and damping, vorticity, confinement, XSPH) run with a block size chosen per
+ * kernel from 64, 128 and 256 threads; results do not depend on it. */
+#define AKUA_PBF_PAIR_KERNELS 6
+int akua_pbf_set_pair_blocks(akua_pbf* solver, const int32_t blocks[AKUA_PBF_PAIR_KERNELS]);
+int akua_pbf_get_pair_blocks(akua_pbf* solver, int32_t blocks[AKUA_PBF_PAIR_KERNELS]);
+/* Autotuner: times every candidate block size of every pair kernel over `steps` profiled steps
+ * (after one warm-up step) started from a copy of the attached records, and keeps the fastest per
+ * kernel (written to blocksOut when not NULL).  The attached records, the step count, pending
+ * captures and the lambda sums are left as they were.  boxMin/boxMax as for akua_pbf_step (NULL
+ * for a batch, whose scenes carry their boxes).  Synchronous. */
+int akua_pbf_autotune(akua_pbf* solver, float deltaTime, const float boxMin[3],
+                      const float boxMax[3], int32_t steps, int32_t* blocksOut);
+
 /* ---- SDF obstacles.  The reference clamps particles to the box and plans a proper boundary in its
  * place (ConstraintSolverCUDA.cu:131-134); here solid shapes given by signed distance functions
  * are added to the box: after each Jacobi correction (and the box clamp) a particle within

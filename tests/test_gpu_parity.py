@@ -346,6 +346,33 @@ def test_step_host_pinned_and_pageable_identical():
     assert pv.tobytes() == pageable.tobytes()
 
 
+def test_autotune_keeps_results_and_user_state():
+    """The autotuner picks block sizes from 64/128/256 on a copy of the records: the attached
+    records and the step count are untouched, and the tuned step gives the same bytes."""
+    import torch
+
+    sc = scene.workload("dam_break_27k", seed=13)
+    cfg, corr = bench_params()
+    ref = sc.particles.copy()
+    with PBFSolver(sc.n, cfg, corr) as s:
+        for _ in range(2):
+            s.step_host(ref, sc.dt, sc.box_min, sc.box_max)
+    buf = torch.from_numpy(sc.particles.view(np.uint8).copy()).cuda()
+    with PBFSolver(sc.n, cfg, corr) as s:
+        s.step(buf, sc.dt, sc.box_min, sc.box_max)
+        before = buf.cpu().numpy().tobytes()
+        steps = s.stats()["steps"]
+        choice = s.autotune(sc.dt, sc.box_min, sc.box_max, steps=2)
+        assert set(choice.values()) <= {64, 128, 256} and s.pair_blocks() == choice
+        assert buf.cpu().numpy().tobytes() == before and s.stats()["steps"] == steps
+        s.step(buf, sc.dt, sc.box_min, sc.box_max)
+        s.set_pair_blocks([64, 256, 64, 256, 64, 256])
+        assert buf.cpu().numpy().view(ak.PARTICLE_DTYPE).tobytes() == ref.tobytes()
+    with pytest.raises(ak.AkuaError):
+        with PBFSolver(sc.n, cfg, corr) as s:
+            s.set_pair_blocks([96] * 6)
+
+
 def test_graph_and_direct_launch_identical():
     sc = scene.dam_break((16, 16, 16), (3.0, 3.0, 3.0), seed=11)
     cfg, corr = bench_params()
