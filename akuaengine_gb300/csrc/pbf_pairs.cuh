@@ -374,7 +374,8 @@ template <bool EXACT>
 __global__ void __launch_bounds__(kMaxPairBlock)
     k_vorticity(const StepParams* __restrict__ P, const float4* __restrict__ x4,
                 const float4* __restrict__ v4, const uint4* __restrict__ nbr4,
-                const uint32_t* __restrict__ cnt, float4* __restrict__ om4) {
+                const uint32_t* __restrict__ cnt, float4* __restrict__ om4,
+                float4* __restrict__ xw4) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P->n) return;
     const StepParams& p = params_for(P, i);
@@ -406,7 +407,9 @@ __global__ void __launch_bounds__(kMaxPairBlock)
             wz = __fmaf_rn(-b.w, cz.y, wz);
         }
     });
-    om4[i] = make_float4(wx, wy, wz, __fsqrt_rn(len2(wx, wy, wz)));
+    const float wn = __fsqrt_rn(len2(wx, wy, wz));
+    om4[i] = make_float4(wx, wy, wz, wn);
+    xw4[i] = make_float4(xi.x, xi.y, xi.z, wn);  // (x, |omega|) for confinement's single gather
 }
 
 // Vorticity confinement (IntegrationCUDA.cu:130-165); writes the confined velocity to a separate
@@ -416,7 +419,8 @@ __global__ void __launch_bounds__(kMaxPairBlock)
     k_confine(const StepParams* __restrict__ P, const float4* __restrict__ x4,
               const float4* __restrict__ v4, const float4* __restrict__ om4,
               const float* __restrict__ rho, const uint4* __restrict__ nbr4,
-              const uint32_t* __restrict__ cnt, float4* __restrict__ vc4) {
+              const uint32_t* __restrict__ cnt, float4* __restrict__ vc4,
+              const float4* __restrict__ xw4, const uint32_t* __restrict__ mass_bits) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P->n) return;
     const StepParams& p = params_for(P, i);
@@ -425,15 +429,14 @@ __global__ void __launch_bounds__(kMaxPairBlock)
     const float4 xi = x4[i], vi = v4[i], wi = om4[i];
     const float rho_i = rho[i];
     float ex = 0.f, ey = 0.f, ez = 0.f;
-    for_each_pair(nbr4 + i, n, (int)cnt[i], [&](uint32_t j0, uint32_t j1, bool two) {
-        const float4 a = __ldg(x4 + j0), b = __ldg(x4 + j1);
-        const float2 wj = make_float2(__ldg(&om4[j0].w), __ldg(&om4[j1].w));
+    // pair term m_j (|omega_i| - |omega_j|) grad W, given positions, masses and |omega_j|
+    auto term = [&](float4 a, float4 b, float2 mj, float2 wj, bool two) {
         const float2 sx = sub2(f2(xi.x), make_float2(a.x, b.x));
         const float2 sy = sub2(f2(xi.y), make_float2(a.y, b.y));
         const float2 sz = sub2(f2(xi.z), make_float2(a.z, b.z));
         float2 gx, gy, gz;
         spiky2<EXACT>(p, sx, sy, sz, len2_2(sx, sy, sz), gx, gy, gz);
-        const float2 s = mul2(make_float2(a.w, b.w), sub2(f2(wi.w), wj));
+        const float2 s = mul2(mj, sub2(f2(wi.w), wj));
         ex = __fmaf_rn(s.x, gx.x, ex);
         ey = __fmaf_rn(s.x, gy.x, ey);
         ez = __fmaf_rn(s.x, gz.x, ez);
@@ -442,7 +445,20 @@ __global__ void __launch_bounds__(kMaxPairBlock)
             ey = __fmaf_rn(s.y, gy.y, ey);
             ez = __fmaf_rn(s.y, gz.y, ez);
         }
-    });
+    };
+    if (__ldg(mass_bits) == 0u) {  // one mass: (x, |omega|) in one gather, the same products
+        const float m = __uint_as_float(__ldg(mass_bits + 1));
+        for_each_pair(nbr4 + i, n, (int)cnt[i], [&](uint32_t j0, uint32_t j1, bool two) {
+            const float4 a = __ldg(xw4 + j0), b = __ldg(xw4 + j1);
+            term(a, b, f2(m), make_float2(a.w, b.w), two);
+        });
+    } else {
+        for_each_pair(nbr4 + i, n, (int)cnt[i], [&](uint32_t j0, uint32_t j1, bool two) {
+            const float4 a = __ldg(x4 + j0), b = __ldg(x4 + j1);
+            term(a, b, make_float2(a.w, b.w),
+                 make_float2(__ldg(&om4[j0].w), __ldg(&om4[j1].w)), two);
+        });
+    }
     const float inv_d = __fdiv_rn(1.0f, rho_i);
     ex = ex * inv_d;
     ey = ey * inv_d;

@@ -362,11 +362,13 @@ void enqueue_pairs(akua_pbf* s, cudaStream_t st, Marker& mark) {
             s->rho, s->lam, 0, s->psl, s->mass_bits);
         mark("k_delta_final");
     }
+    // psl is free after the last delta: it carries (x, |omega|) to confinement
     akua::k_vorticity<EXACT><<<gp(3), pb[3], 0, st>>>(s->d_params, s->x4, s->v4, nbr4,
-                                                              s->cnt, s->om4);
+                                                      s->cnt, s->om4, s->psl);
     mark("k_vorticity");
     akua::k_confine<EXACT><<<gp(4), pb[4], 0, st>>>(s->d_params, s->x4, s->v4, s->om4,
-                                                            s->rho, nbr4, s->cnt, s->vc4);
+                                                    s->rho, nbr4, s->cnt, s->vc4, s->psl,
+                                                    s->mass_bits);
     mark("k_confine");
     akua::k_xsph<<<gp(5), pb[5], 0, st>>>(s->d_params, s->x4, s->vc4, nbr4, s->cnt, s->v4);
     mark("k_xsph");
