@@ -489,7 +489,8 @@ def run_ours(args, sc, cfg, corr):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        sps, psps, cores, sample = time_oracle(sc, cfg, corr, 3, 30.0)
+        # ~10 s of CPU work at 1M on 16 cores (18 steps); larger scenes fall back to a sub-block
+        sps, psps, cores, sample = time_oracle(sc, cfg, corr, 18, 30.0)
         cpu = {"value": sps, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
                "particle_steps_per_s": psps}
 
