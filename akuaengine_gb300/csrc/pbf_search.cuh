@@ -19,7 +19,9 @@
 // buckets are contiguous runs), and every particle of the run tests the whole chunk at once; a
 // ballot and a population count place each hit at the particle's running count plus the hits of
 // lower lanes, which is the reference's order.  Each candidate is loaded once per run instead of
-// once per particle, and no lane idles on another lane's bucket length.
+// once per particle, and no lane idles on another lane's bucket length.  Two particles are tested
+// per round (independent ballots and placements, distances in packed FP32x2): their dependency
+// chains interleave, which a lane-serial walk or a windowed one (both measured slower) cannot.
 //
 // The first kListStage entries of each list are staged in shared memory and written out as
 // coalesced uint4 tiles (pbf_pairs.cuh).  When `density` is set, the first Jacobi iteration's
@@ -119,7 +121,8 @@ __global__ void __launch_bounds__(kSearchBlock)
             const uint32_t by = __shfl_sync(kFullWarp, e.y, b);
             const uint32_t bo = __shfl_sync(kFullWarp, off, b);
             const bool live = at < total;
-            float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+            float4 c = make_float4(__int_as_float(0x7f800000), __int_as_float(0x7f800000),
+                                   __int_as_float(0x7f800000), 0.f);
             uint32_t j = 0xffffffffu;
             if (live) {
                 const uint32_t t = bx + (at - bo);
@@ -131,16 +134,35 @@ __global__ void __launch_bounds__(kSearchBlock)
                     j = t;
                 }
             }
-            for (int q = q0; q < q1; ++q) {
+            // two particles per round: independent tests, ballots and placements
+            const uint32_t jrel = j - (uint32_t)base;  // == q for particle q's own slot
+            const float2 cxx = f2(c.x), cyy = f2(c.y), czz = f2(c.z);
+            auto place = [&](int q, int pos) {
+                if (pos < kListStage) rows[q * kListRow + pos] = j;
+                else if (pos < cap) nbr[4 * ((size_t)(pos >> 2) * n + base + q) + (pos & 3)] = j;
+            };
+            int q = q0;
+            for (; q + 1 < q1; q += 2) {
+                const float4 xa = xs[q], xb = xs[q + 1];
+                const float2 d2 = len2_2(sub2(make_float2(xa.x, xb.x), cxx),
+                                         sub2(make_float2(xa.y, xb.y), cyy),
+                                         sub2(make_float2(xa.z, xb.z), czz));
+                const bool ha = d2.x < h2 && jrel != (uint32_t)q;
+                const bool hb = d2.y < h2 && jrel != (uint32_t)(q + 1);
+                const uint32_t ba = __ballot_sync(kFullWarp, ha);
+                const uint32_t bb = __ballot_sync(kFullWarp, hb);
+                const int pa = __shfl_sync(kFullWarp, count, q) + __popc(ba & below);
+                const int pb = __shfl_sync(kFullWarp, count, q + 1) + __popc(bb & below);
+                if (ha) place(q, pa);
+                if (hb) place(q + 1, pb);
+                count += lane == q ? __popc(ba) : (lane == q + 1 ? __popc(bb) : 0);
+            }
+            if (q < q1) {
                 const float4 xq = xs[q];
-                const float sx = xq.x - c.x, sy = xq.y - c.y, sz = xq.z - c.z;
-                const bool hit = live && len2(sx, sy, sz) < h2 && j != (uint32_t)(base + q);
+                const bool hit = len2(xq.x - c.x, xq.y - c.y, xq.z - c.z) < h2 && jrel != (uint32_t)q;
                 const uint32_t bal = __ballot_sync(kFullWarp, hit);
                 const int pos = __shfl_sync(kFullWarp, count, q) + __popc(bal & below);
-                if (hit) {
-                    if (pos < kListStage) rows[q * kListRow + pos] = j;
-                    else if (pos < cap) nbr[4 * ((size_t)(pos >> 2) * n + base + q) + (pos & 3)] = j;
-                }
+                if (hit) place(q, pos);
                 if (lane == q) count += __popc(bal);
             }
         }
