@@ -83,6 +83,20 @@ __device__ __forceinline__ void for_each_pair(const uint4* __restrict__ col, int
     }
 }
 
+// A particle's two-float4 record (x.xyz, w0 | v.xyz, w1) read in one 256-bit load (32-byte
+// aligned: record j starts at float4 2j of a cudaMalloc'd array).
+struct Rec8 {
+    float4 x, v;
+};
+__device__ __forceinline__ Rec8 ld_rec8(const float4* __restrict__ rec, uint32_t j) {
+    Rec8 r;
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(r.x.x), "=f"(r.x.y), "=f"(r.x.z), "=f"(r.x.w), "=f"(r.v.x), "=f"(r.v.y),
+          "=f"(r.v.z), "=f"(r.v.w)
+        : "l"(rec + 2 * (size_t)j));
+    return r;
+}
+
 // Density and lambda accumulators (ConstraintSolverCUDA.cu:16-97), two neighbours per call.
 template <bool EXACT>
 struct DensityLambda2 {
@@ -311,7 +325,8 @@ __global__ void __launch_bounds__(kMaxPairBlock)
                   uint32_t* __restrict__ rref, const float* __restrict__ rho_c,
                   const float* __restrict__ lam_c, const float4* __restrict__ dp_c,
                   float* __restrict__ rho, float* __restrict__ lam_out, int has_delta,
-                  const float4* __restrict__ psl, const uint32_t* __restrict__ mass_bits) {
+                  const float4* __restrict__ psl, const uint32_t* __restrict__ mass_bits,
+                  float4* __restrict__ xv8) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P->n) return;
     const StepParams& p = params_for(P, i);
@@ -361,8 +376,11 @@ __global__ void __launch_bounds__(kMaxPairBlock)
             }
         }
     }
-    x4[i] = make_float4(nx, ny, nz, xi.w);
-    v4[i] = make_float4(vx, vy, vz, 0.f);
+    const float4 xn = make_float4(nx, ny, nz, xi.w), vn = make_float4(vx, vy, vz, 0.f);
+    x4[i] = xn;
+    v4[i] = vn;
+    xv8[2 * (size_t)i] = xn;  // (x, m | v) for vorticity's single gather
+    xv8[2 * (size_t)i + 1] = vn;
     col4[i] = col4g[i];
     size[i] = sizeg[i];
     rref[i] = rref_new[i];
@@ -373,9 +391,9 @@ __global__ void __launch_bounds__(kMaxPairBlock)
 template <bool EXACT>
 __global__ void __launch_bounds__(kMaxPairBlock)
     k_vorticity(const StepParams* __restrict__ P, const float4* __restrict__ x4,
-                const float4* __restrict__ v4, const uint4* __restrict__ nbr4,
-                const uint32_t* __restrict__ cnt, float4* __restrict__ om4,
-                float4* __restrict__ xw4) {
+                const float4* __restrict__ v4, const float4* __restrict__ xv8,
+                const uint4* __restrict__ nbr4, const uint32_t* __restrict__ cnt,
+                float4* __restrict__ om4, float4* __restrict__ xw4) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P->n) return;
     const StepParams& p = params_for(P, i);
@@ -384,8 +402,8 @@ __global__ void __launch_bounds__(kMaxPairBlock)
     const float4 xi = x4[i], vi = v4[i];
     float wx = 0.f, wy = 0.f, wz = 0.f;
     for_each_pair(nbr4 + i, n, (int)cnt[i], [&](uint32_t j0, uint32_t j1, bool two) {
-        const float4 a = __ldg(x4 + j0), b = __ldg(x4 + j1);
-        const float4 va = __ldg(v4 + j0), vb = __ldg(v4 + j1);
+        const Rec8 ra = ld_rec8(xv8, j0), rb = ld_rec8(xv8, j1);
+        const float4 a = ra.x, b = rb.x, va = ra.v, vb = rb.v;
         const float2 sx = sub2(f2(xi.x), make_float2(a.x, b.x));
         const float2 sy = sub2(f2(xi.y), make_float2(a.y, b.y));
         const float2 sz = sub2(f2(xi.z), make_float2(a.z, b.z));
@@ -412,14 +430,14 @@ __global__ void __launch_bounds__(kMaxPairBlock)
     xw4[i] = make_float4(xi.x, xi.y, xi.z, wn);  // (x, |omega|) for confinement's single gather
 }
 
-// Vorticity confinement (IntegrationCUDA.cu:130-165); writes the confined velocity to a separate
-// buffer with vc4.w = m_i / rho_i for the XSPH pass.
+// Vorticity confinement (IntegrationCUDA.cu:130-165); writes the confined velocity to the
+// particle records (x, m_i / rho_i | v) for the XSPH pass.
 template <bool EXACT>
 __global__ void __launch_bounds__(kMaxPairBlock)
     k_confine(const StepParams* __restrict__ P, const float4* __restrict__ x4,
               const float4* __restrict__ v4, const float4* __restrict__ om4,
               const float* __restrict__ rho, const uint4* __restrict__ nbr4,
-              const uint32_t* __restrict__ cnt, float4* __restrict__ vc4,
+              const uint32_t* __restrict__ cnt, float4* __restrict__ xv8,
               const float4* __restrict__ xw4, const uint32_t* __restrict__ mass_bits) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P->n) return;
@@ -478,29 +496,34 @@ __global__ void __launch_bounds__(kMaxPairBlock)
         vy = __fmaf_rn(p.dt, p.vort_eps * cr.y, vy);
         vz = __fmaf_rn(p.dt, p.vort_eps * cr.z, vz);
     }
-    vc4[i] = make_float4(vx, vy, vz, __fdiv_rn(xi.w, rho_i));
+    // (x, m_i / rho_i | confined v) for XSPH's single gather; vorticity, the only other reader of
+    // these records, has finished, and no thread here reads another particle's record
+    xv8[2 * (size_t)i] = make_float4(xi.x, xi.y, xi.z, __fdiv_rn(xi.w, rho_i));
+    xv8[2 * (size_t)i + 1] = make_float4(vx, vy, vz, 0.f);
 }
 
-// XSPH viscosity (IntegrationCUDA.cu:167-195) from the confined-velocity snapshot vc4.
+// XSPH viscosity (IntegrationCUDA.cu:167-195) from the confined-velocity snapshot in the records
+// (x, m / rho | v).
 __global__ void __launch_bounds__(kMaxPairBlock)
-    k_xsph(const StepParams* __restrict__ P, const float4* __restrict__ x4,
-           const float4* __restrict__ vc4, const uint4* __restrict__ nbr4,
-           const uint32_t* __restrict__ cnt, float4* __restrict__ v4) {
+    k_xsph(const StepParams* __restrict__ P, const float4* __restrict__ xv8,
+           const uint4* __restrict__ nbr4, const uint32_t* __restrict__ cnt,
+           float4* __restrict__ v4) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P->n) return;
     const StepParams& p = params_for(P, i);
     const int n = p.n;
     if (i >= n) return;
-    const float4 xi = x4[i], vi = vc4[i];
+    const Rec8 ri = ld_rec8(xv8, (uint32_t)i);
+    const float4 xi = ri.x, vi = ri.v;
     float ax = 0.f, ay = 0.f, az = 0.f;
     for_each_pair(nbr4 + i, n, (int)cnt[i], [&](uint32_t j0, uint32_t j1, bool two) {
-        const float4 a = __ldg(x4 + j0), b = __ldg(x4 + j1);
-        const float4 va = __ldg(vc4 + j0), vb = __ldg(vc4 + j1);
+        const Rec8 ra = ld_rec8(xv8, j0), rb = ld_rec8(xv8, j1);
+        const float4 a = ra.x, b = rb.x, va = ra.v, vb = rb.v;
         const float2 sx = sub2(f2(xi.x), make_float2(a.x, b.x));
         const float2 sy = sub2(f2(xi.y), make_float2(a.y, b.y));
         const float2 sz = sub2(f2(xi.z), make_float2(a.z, b.z));
         const float2 w = poly6_2(p, len2_2(sx, sy, sz));
-        const float2 s = make_float2(va.w, vb.w);
+        const float2 s = make_float2(a.w, b.w);  // m_j / rho_j
         const float2 tx = mul2(s, sub2(make_float2(va.x, vb.x), f2(vi.x)));
         const float2 ty = mul2(s, sub2(make_float2(va.y, vb.y), f2(vi.y)));
         const float2 tz = mul2(s, sub2(make_float2(va.z, vb.z), f2(vi.z)));

@@ -54,7 +54,7 @@ struct akua_pbf {
     float4* dp4 = nullptr;
     // gathered copies and per-step arrays
     float4 *x4g = nullptr, *col4g = nullptr, *ps0 = nullptr, *ps1 = nullptr;
-    float4 *vstar4 = nullptr, *om4 = nullptr, *vc4 = nullptr, *dpg = nullptr, *xref = nullptr;
+    float4 *vstar4 = nullptr, *om4 = nullptr, *xv8 = nullptr, *dpg = nullptr, *xref = nullptr;
     float *sizeg = nullptr, *rhog = nullptr, *lamg = nullptr;
     uint32_t *rrefg = nullptr, *rank_of_import = nullptr, *r2i = nullptr, *blen = nullptr, *order = nullptr;
     uint32_t* bmix = nullptr;  // per bucket start: nonzero when the bucket is not one internal run
@@ -145,7 +145,7 @@ cudaError_t dalloc(akua_pbf* s, T** p, size_t count) {
 
 void free_all(akua_pbf* s) {
     void* ptrs[] = {s->d_params, s->x4, s->v4, s->col4, s->size, s->rref, s->rho, s->lam, s->dp4,
-                    s->x4g, s->col4g, s->ps0, s->ps1, s->vstar4, s->om4, s->vc4, s->dpg, s->xref,
+                    s->x4g, s->col4g, s->ps0, s->ps1, s->vstar4, s->om4, s->xv8, s->dpg, s->xref,
                     s->sizeg, s->rhog, s->lamg, s->rrefg, s->rank_of_import, s->r2i, s->blen, s->order, s->bmix,
                     s->ka0, s->va0, s->ka1, s->va1, s->kb0, s->vb0, s->kb1, s->vb1,
                     s->sort_scratch, s->sort_scratch_b, s->table, s->nbr, s->cnt, s->flags,
@@ -351,7 +351,7 @@ void enqueue_pairs(akua_pbf* s, cudaStream_t st, Marker& mark) {
             akua::k_delta_final<EXACT><<<gp(2), pb[2], 0, st>>>(
                 s->d_params, cur, s->lam, nbr4, s->cnt, s->x4g, s->x4, s->v4, s->vstar4, s->dp4,
                 s->col4g, s->sizeg, s->col4, s->size, s->rrefg, s->rref, s->rhog, s->lamg, s->dpg,
-                s->rho, s->lam, 1, s->psl, s->mass_bits);
+                s->rho, s->lam, 1, s->psl, s->mass_bits, s->xv8);
             mark("k_delta_final");
         }
     }
@@ -359,18 +359,18 @@ void enqueue_pairs(akua_pbf* s, cudaStream_t st, Marker& mark) {
         akua::k_delta_final<EXACT><<<gp(2), pb[2], 0, st>>>(
             s->d_params, s->ps0, s->lam, nbr4, s->cnt, s->x4g, s->x4, s->v4, s->vstar4, s->dp4,
             s->col4g, s->sizeg, s->col4, s->size, s->rrefg, s->rref, s->rhog, s->lamg, s->dpg,
-            s->rho, s->lam, 0, s->psl, s->mass_bits);
+            s->rho, s->lam, 0, s->psl, s->mass_bits, s->xv8);
         mark("k_delta_final");
     }
     // psl is free after the last delta: it carries (x, |omega|) to confinement
-    akua::k_vorticity<EXACT><<<gp(3), pb[3], 0, st>>>(s->d_params, s->x4, s->v4, nbr4,
+    akua::k_vorticity<EXACT><<<gp(3), pb[3], 0, st>>>(s->d_params, s->x4, s->v4, s->xv8, nbr4,
                                                       s->cnt, s->om4, s->psl);
     mark("k_vorticity");
     akua::k_confine<EXACT><<<gp(4), pb[4], 0, st>>>(s->d_params, s->x4, s->v4, s->om4,
-                                                    s->rho, nbr4, s->cnt, s->vc4, s->psl,
+                                                    s->rho, nbr4, s->cnt, s->xv8, s->psl,
                                                     s->mass_bits);
     mark("k_confine");
-    akua::k_xsph<<<gp(5), pb[5], 0, st>>>(s->d_params, s->x4, s->vc4, nbr4, s->cnt, s->v4);
+    akua::k_xsph<<<gp(5), pb[5], 0, st>>>(s->d_params, s->xv8, nbr4, s->cnt, s->v4);
     mark("k_xsph");
 }
 
@@ -631,7 +631,7 @@ int create_solver(int32_t n, const akua_pbf_config* cfg, const akua_lambda_corr_
     chk(dalloc(s, &s->rho, N)); chk(dalloc(s, &s->lam, N)); chk(dalloc(s, &s->dp4, N));
     chk(dalloc(s, &s->x4g, N)); chk(dalloc(s, &s->col4g, N));
     chk(dalloc(s, &s->ps0, N)); chk(dalloc(s, &s->ps1, N));
-    chk(dalloc(s, &s->vstar4, N)); chk(dalloc(s, &s->om4, N)); chk(dalloc(s, &s->vc4, N));
+    chk(dalloc(s, &s->vstar4, N)); chk(dalloc(s, &s->om4, N)); chk(dalloc(s, &s->xv8, 2 * N));
     chk(dalloc(s, &s->dpg, N)); chk(dalloc(s, &s->xref, N));
     chk(dalloc(s, &s->sizeg, N)); chk(dalloc(s, &s->rhog, N)); chk(dalloc(s, &s->lamg, N));
     chk(dalloc(s, &s->rrefg, N)); chk(dalloc(s, &s->rank_of_import, N)); chk(dalloc(s, &s->r2i, N));

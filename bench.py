@@ -46,24 +46,27 @@ KERNEL_BYTES = {
     "k_keys": lambda L, B: 16 + 16 + 4 + 12,
     "radix_upsweep": lambda L, B: 4,                  # R key (per pass)
     "radix_downsweep": lambda L, B: 16,               # R key, value; W key, value (per pass)
-    "k_morton_ref": lambda L, B: 12,                  # R permutation, Morton key; W key
+    "k_rank_scatter": lambda L, B: 8,                 # R reference permutation; W slot rank
     # R two permutations, x|m, v, colour, size, old rank; W x|m, colour, size, x*|m, rank->slot,
     # slot->rank, reference-ordered x*|m, order
     "k_gather": lambda L, B: 8 + 16 + 16 + 16 + 4 + 4 + 16 + 16 + 4 + 16 + 4 + 4 + 16 + 4,
     "k_ref_table": lambda L, B: 4 + 12 * B,           # R keys; W bucket starts, flags
     "k_bucket_meta": lambda L, B: 4 + 4 + 12 * B,     # R keys, slots; W lengths, flags
     "k_table_fill": lambda L, B: 4 + 24 * B,          # R keys; R slot, length, flag; W entry
-    # R x*|m, 27 bucket entries per cell run; W lists, count, rho, lambda
-    "k_search": lambda L, B: 16 + 27 * 8 * B + L + 4 + 8,
+    # R x*|m, 27 bucket entries per cell run; W lists, count, rho, lambda, x*|lambda
+    "k_search": lambda L, B: 16 + 27 * 8 * B + L + 4 + 8 + 16,
     "k_table_clear": lambda L, B: 4 + 8 * B,          # R keys; W entry
-    "k_density_lambda": lambda L, B: 16 + 4 + L + 8,  # R x*|m, count, lists; W rho, lambda
+    # R x*|m, count, lists; W rho, lambda, x*|lambda
+    "k_density_lambda": lambda L, B: 16 + 4 + L + 8 + 16,
     # R x*|m, lambda, count, lists; W x*|m, delta
     "k_delta_correct": lambda L, B: 16 + 4 + 4 + L + 16 + 16,
-    # R x*|m, lambda, count, lists, x|m, colour, size, rank; W x, v, v*, delta, colour, size, rank
-    "k_delta_final": lambda L, B: 16 + 4 + 4 + L + 16 + 16 + 4 + 4 + 16 * 4 + 16 + 4 + 4,
-    "k_vorticity": lambda L, B: 16 + 16 + 4 + L + 16,        # R x, v, count, lists; W omega
-    "k_confine": lambda L, B: 16 + 16 + 16 + 4 + 4 + L + 16,  # R x, v, omega, rho, count, lists; W v|m/rho
-    "k_xsph": lambda L, B: 16 + 16 + 4 + L + 16,             # R x, v|m/rho, count, lists; W v
+    # R x*|m, lambda, count, lists, x|m, colour, size, rank; W x, v, v*, delta, colour, size, rank,
+    # record (x|m, v)
+    "k_delta_final": lambda L, B: 16 + 4 + 4 + L + 16 + 16 + 4 + 4 + 16 * 4 + 16 + 4 + 4 + 32,
+    "k_vorticity": lambda L, B: 16 + 16 + 4 + L + 16 + 16,   # R x, v, count, lists; W omega, x|omega
+    # R x, v, omega, rho, count, lists; W record (x|m/rho, v)
+    "k_confine": lambda L, B: 16 + 16 + 16 + 4 + 4 + L + 32,
+    "k_xsph": lambda L, B: 32 + 4 + L + 16,                  # R record, count, lists; W v
     # R slot, key, x, v, v*, delta, omega, colour, rho, lambda, size; W record 108
     "k_export": lambda L, B: 4 + 4 + 16 * 6 + 4 + 4 + 4 + 108,
 }
