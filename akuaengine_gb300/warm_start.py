@@ -253,18 +253,24 @@ def rollout_errors(sc, cfg, corr, iterations: int, net=None, steps: int = 60, st
 
 def calibrate_blend(net: LambdaNet, sc, cfg, corr, iterations: int,
                     blends=(0.0, 0.05, 0.1, 0.15, 0.2, 0.3, 0.4, 0.5), steps: int = 60,
-                    stream=None) -> dict:
-    """Picks the blend whose rollout of `sc` has the lowest per-step max density error averaged
-    over the rollout (mean |C| breaks ties) and sets it; blend 0 is the plain solver, so the
-    choice is never worse than plain on that rollout.  Returns {blend: (mean of max C, mean of
-    mean |C|)}."""
+                    stream=None, max_tolerance: float | None = None) -> dict:
+    """Rolls `sc` out with each blend and sets the best one.  Errors per rollout: the per-step
+    max density error and mean |C|, each averaged over the rollout.  Without `max_tolerance` the
+    best blend has the lowest max error (mean |C| breaks ties).  With it, the best blend has the
+    lowest mean |C| among those whose max error is at most (1 + max_tolerance) times blend 0's.
+    Blend 0 is the plain solver, so in both cases the choice is no worse than plain on that
+    rollout by those measures.  Returns {blend: (mean of max C, mean of mean |C|)}."""
     res = {}
-    for g in blends:
+    for g in sorted(set(float(b) for b in blends) | {0.0}):
         net.set_blend(g)
         e = rollout_errors(sc, cfg, corr, iterations, net, steps, stream)
         bad = not np.isfinite(e).all()
-        res[float(g)] = (float("inf"), float("inf")) if bad else (float(e[:, 0].mean()),
-                                                                  float(e[:, 1].mean()))
-    best = min(res, key=lambda g: (res[g][0], res[g][1]))
+        res[g] = (float("inf"), float("inf")) if bad else (float(e[:, 0].mean()),
+                                                           float(e[:, 1].mean()))
+    if max_tolerance is None:
+        best = min(res, key=lambda g: (res[g][0], res[g][1]))
+    else:
+        bound = (1.0 + max_tolerance) * res[0.0][0]
+        best = min((g for g in res if res[g][0] <= bound), key=lambda g: (res[g][1], res[g][0]))
     net.set_blend(best)
     return res

@@ -105,3 +105,23 @@ def test_warm_start_launches_the_network(trained):
         counts.append(s.kernels_per_step())
         s.close()
     assert counts[1] == counts[0] + 1  # the network's forward pass; features come from the walk
+
+
+def test_calibration_on_mean_error_within_max_bound(trained):
+    """With a max-error tolerance the chosen blend has the lowest mean |C| among the blends
+    whose max C stays within the bound of blend 0 (the plain solver), which is one of them."""
+    from akuaengine_gb300.warm_start import calibrate_blend
+
+    net = trained[0]
+    before = net.blend
+    sc = scene.workload("dam_break_27k", seed=0)
+    cfg, corr = scene.benchmark_params()
+    cal = calibrate_blend(net, sc, cfg, corr, iterations=2, steps=60, blends=(0.5, 1.0),
+                          max_tolerance=0.05)
+    b = net.blend
+    bound = 1.05 * cal[0.0][0]
+    print("calibration within the max bound: %s -> %.2f" % (cal, b))
+    assert set(cal) == {0.0, 0.5, 1.0}
+    assert cal[b][0] <= bound
+    assert all(cal[b][1] <= cal[g][1] for g in cal if cal[g][0] <= bound)
+    net.set_blend(before)
