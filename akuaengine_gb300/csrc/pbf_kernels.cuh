@@ -10,7 +10,7 @@
 //     neighbour passes use it.  It is a stable sort over the previous reference order, so it does
 //     not wait for the hash sort: particles of one cell share their hash, so their order within
 //     the cell is their new reference order either way (cells that share a clamped Morton key
-//     and are not contiguous are found by k_bucket_meta and walked by rank).
+//     and are not contiguous are found by k_table_build and walked by rank).
 // Results do not depend on the internal order: every per-particle sum runs over the neighbour list
 // in the reference's walk order.
 //
@@ -18,7 +18,7 @@
 //   predict              IntegrationCUDA.cu:27-36            k_keys, k_gather
 //   cell hash            NeighbourSearchCUDA.cu:15-44        k_keys
 //   sort by hash         NeighbourSearchCUDA.cu:167-170      radix sort of (hash, previous rank)
-//   bucket starts        NeighbourSearchCUDA.cu:52-65        k_ref_table, k_bucket_meta, k_table_fill
+//   bucket starts        NeighbourSearchCUDA.cu:52-65        k_table_build
 //   neighbour walk       NeighbourSearchCUDA.cu:72-130       k_search (+ iteration 1 density/lambda)
 //   density, lambda      ConstraintSolverCUDA.cu:16-97       k_search / k_density_lambda
 //   delta, correct       ConstraintSolverCUDA.cu:99-169      k_delta_correct / k_delta_final
@@ -241,53 +241,34 @@ __global__ void __launch_bounds__(kElemBlock)
 
 // The bucket table (NeighbourSearchCUDA.cu:52-65 builds hash -> first sorted index).  Here an
 // entry is (x, y): y = 0 for a hash no particle carries; otherwise y = bucket length and x = the
-// bucket's first internal slot, or, with bit 31 of y set (a mixed bucket, see k_bucket_meta), its
+// bucket's first internal slot, or, with bit 31 of y set (a mixed bucket, see k_table_build), its
 // first reference rank.  The table is all-empty between steps: k_table_clear empties this step's
 // entries after the walk.
 
-// Bucket starts: table[hash].x = first rank carrying it (read by k_bucket_meta); clears the
-// bucket's mixed flag.
+// One thread per bucket start (the first reference rank carrying a hash) reads its bucket's ranks
+// (a short run of the sorted keys) and writes the entry: the length, and whether the bucket's
+// particles are one contiguous run of internal slots in rank order (then x = the first slot) or
+// not (several cells share the hash, or clamped cells share a Morton key: x = the first rank,
+// mixed bit set).
 __global__ void __launch_bounds__(kElemBlock)
-    k_ref_table(const StepParams* __restrict__ P, const uint32_t* __restrict__ kr,
-                uint2* __restrict__ table, uint32_t* __restrict__ bmix) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= P->n) return;
-    const uint32_t k = kr[r];
-    if (r == 0 || kr[r - 1] != k) {
-        table[k] = make_uint2((uint32_t)r, 0u);
-        bmix[r] = 0u;
-    }
-}
-
-// blen[start] = number of ranks in the bucket; bmix[start] != 0 when the bucket's particles are
-// not one contiguous run of internal slots in rank order (several cells share its hash, or
-// clamped cells share a Morton key).
-__global__ void __launch_bounds__(kElemBlock)
-    k_bucket_meta(const StepParams* __restrict__ P, const uint32_t* __restrict__ kr,
-                  const uint2* __restrict__ table, const uint32_t* __restrict__ r2i,
-                  uint32_t* __restrict__ blen, uint32_t* __restrict__ bmix) {
+    k_table_build(const StepParams* __restrict__ P, const uint32_t* __restrict__ kr,
+                  const uint32_t* __restrict__ r2i, uint2* __restrict__ table) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = P->n;
     if (r >= n) return;
     const uint32_t k = kr[r];
-    const bool first = r == 0 || kr[r - 1] != k;
-    const uint32_t start = first ? (uint32_t)r : table[k].x;
-    if (!first && r2i[r] != r2i[r - 1] + 1u) atomicOr(&bmix[start], 1u);
-    if (r == n - 1 || kr[r + 1] != k) blen[start] = (uint32_t)r + 1u - start;
-}
-
-// Final table entries for the walk.
-__global__ void __launch_bounds__(kElemBlock)
-    k_table_fill(const StepParams* __restrict__ P, const uint32_t* __restrict__ kr,
-                 const uint32_t* __restrict__ r2i, const uint32_t* __restrict__ blen,
-                 const uint32_t* __restrict__ bmix, uint2* __restrict__ table) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= P->n) return;
-    const uint32_t k = kr[r];
-    if (r == 0 || kr[r - 1] != k) {
-        const uint32_t len = blen[r];
-        table[k] = bmix[r] ? make_uint2((uint32_t)r, len | kMixedBucket) : make_uint2(r2i[r], len);
+    if (r > 0 && kr[r - 1] == k) return;
+    const uint32_t s0 = r2i[r];
+    uint32_t prev = s0;
+    bool run = true;
+    int e = r + 1;
+    for (; e < n && kr[e] == k; ++e) {
+        const uint32_t se = r2i[e];
+        run = run && se == prev + 1u;
+        prev = se;
     }
+    const uint32_t len = (uint32_t)(e - r);
+    table[k] = run ? make_uint2(s0, len) : make_uint2((uint32_t)r, len | kMixedBucket);
 }
 
 // Empties this step's entries, leaving the table all-empty for the next step.

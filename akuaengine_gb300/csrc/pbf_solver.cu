@@ -56,8 +56,7 @@ struct akua_pbf {
     float4 *x4g = nullptr, *col4g = nullptr, *ps0 = nullptr, *ps1 = nullptr;
     float4 *vstar4 = nullptr, *om4 = nullptr, *xv8 = nullptr, *dpg = nullptr, *xref = nullptr;
     float *sizeg = nullptr, *rhog = nullptr, *lamg = nullptr;
-    uint32_t *rrefg = nullptr, *rank_of_import = nullptr, *r2i = nullptr, *blen = nullptr, *order = nullptr;
-    uint32_t* bmix = nullptr;  // per bucket start: nonzero when the bucket is not one internal run
+    uint32_t *rrefg = nullptr, *rank_of_import = nullptr, *r2i = nullptr, *order = nullptr;
     // sorts: reference order (A) and Morton order (B)
     uint32_t *ka0 = nullptr, *va0 = nullptr, *ka1 = nullptr, *va1 = nullptr;
     uint32_t *kb0 = nullptr, *vb0 = nullptr, *kb1 = nullptr, *vb1 = nullptr;
@@ -146,7 +145,7 @@ cudaError_t dalloc(akua_pbf* s, T** p, size_t count) {
 void free_all(akua_pbf* s) {
     void* ptrs[] = {s->d_params, s->x4, s->v4, s->col4, s->size, s->rref, s->rho, s->lam, s->dp4,
                     s->x4g, s->col4g, s->ps0, s->ps1, s->vstar4, s->om4, s->xv8, s->dpg, s->xref,
-                    s->sizeg, s->rhog, s->lamg, s->rrefg, s->rank_of_import, s->r2i, s->blen, s->order, s->bmix,
+                    s->sizeg, s->rhog, s->lamg, s->rrefg, s->rank_of_import, s->r2i, s->order,
                     s->ka0, s->va0, s->ka1, s->va1, s->kb0, s->vb0, s->kb1, s->vb1,
                     s->sort_scratch, s->sort_scratch_b, s->table, s->nbr, s->cnt, s->flags,
                     s->staging,
@@ -414,14 +413,8 @@ void enqueue_body(akua_pbf* s, cudaStream_t st, const char* aos, size_t stride, 
         s->rhog, s->lamg, s->dpg, carry ? 1 : 0, s->lacc, s->lprev,
         learn_mode(s) ? s->speed : nullptr, s->mass_bits);
     mark("k_gather");
-    akua::k_ref_table<<<ge, akua::kElemBlock, 0, st>>>(s->d_params, s->kr, s->table, s->bmix);
-    mark("k_ref_table");
-    akua::k_bucket_meta<<<ge, akua::kElemBlock, 0, st>>>(s->d_params, s->kr, s->table, s->r2i,
-                                                         s->blen, s->bmix);
-    mark("k_bucket_meta");
-    akua::k_table_fill<<<ge, akua::kElemBlock, 0, st>>>(s->d_params, s->kr, s->r2i, s->blen,
-                                                        s->bmix, s->table);
-    mark("k_table_fill");
+    akua::k_table_build<<<ge, akua::kElemBlock, 0, st>>>(s->d_params, s->kr, s->r2i, s->table);
+    mark("k_table_build");
     if (s->options & AKUA_PBF_OPT_EXACT_MATH) enqueue_pairs<true>(s, st, mark);
     else enqueue_pairs<false>(s, st, mark);
     if (aos) {
@@ -635,8 +628,7 @@ int create_solver(int32_t n, const akua_pbf_config* cfg, const akua_lambda_corr_
     chk(dalloc(s, &s->dpg, N)); chk(dalloc(s, &s->xref, N));
     chk(dalloc(s, &s->sizeg, N)); chk(dalloc(s, &s->rhog, N)); chk(dalloc(s, &s->lamg, N));
     chk(dalloc(s, &s->rrefg, N)); chk(dalloc(s, &s->rank_of_import, N)); chk(dalloc(s, &s->r2i, N));
-    chk(dalloc(s, &s->bmix, N));
-    chk(dalloc(s, &s->blen, N)); chk(dalloc(s, &s->order, N));
+    chk(dalloc(s, &s->order, N));
     chk(dalloc(s, &s->ka0, N)); chk(dalloc(s, &s->va0, N));
     chk(dalloc(s, &s->ka1, N)); chk(dalloc(s, &s->va1, N));
     chk(dalloc(s, &s->kb0, N)); chk(dalloc(s, &s->vb0, N));

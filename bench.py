@@ -50,9 +50,7 @@ KERNEL_BYTES = {
     # R two permutations, x|m, v, colour, size, old rank; W x|m, colour, size, x*|m, rank->slot,
     # slot->rank, reference-ordered x*|m, order
     "k_gather": lambda L, B: 8 + 16 + 16 + 16 + 4 + 4 + 16 + 16 + 4 + 16 + 4 + 4 + 16 + 4,
-    "k_ref_table": lambda L, B: 4 + 12 * B,           # R keys; W bucket starts, flags
-    "k_bucket_meta": lambda L, B: 4 + 4 + 12 * B,     # R keys, slots; W lengths, flags
-    "k_table_fill": lambda L, B: 4 + 24 * B,          # R keys; R slot, length, flag; W entry
+    "k_table_build": lambda L, B: 4 + 4 + 8 * B,      # R keys, slots; W entry
     # R x*|m, 27 bucket entries per cell run; W lists, count, rho, lambda, x*|lambda
     "k_search": lambda L, B: 16 + 27 * 8 * B + L + 4 + 8 + 16,
     "k_table_clear": lambda L, B: 4 + 8 * B,          # R keys; W entry
