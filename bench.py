@@ -31,6 +31,13 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 METRIC = "1M-particle PBF steps/s"
+# per workload: metric name, lattice block(s), box in block widths
+WORKLOADS = {
+    "dam_break_27k": ("27k-particle PBF steps/s", [30, 30, 30], [4.0, 4.0, 4.0]),
+    "dam_break_1m": (METRIC, [100, 100, 100], [3.0, 1.5, 1.5]),
+    "double_dam_break_8m": ("8M-particle PBF steps/s", [[200, 100, 200], [200, 100, 200]],
+                            [6.0, 2.0, 2.0]),
+}
 UNIT = "steps/s"
 WORKLOAD = "dam_break_1m"
 
@@ -195,7 +202,8 @@ def run_reference(args, sc, cfg, corr):
     # warm-up: W steps of a small sample (the oracle has no caches to warm beyond the first call)
     sps, psps, cores, sample = time_oracle(sc, cfg, corr, args.steps, budget)
     line = {
-        "impl": "reference", "metric": METRIC, "value": sps, "unit": UNIT, "n_gpus": args.gpus,
+        "impl": "reference", "metric": WORKLOADS[args.workload][0], "value": sps, "unit": UNIT,
+        "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / sps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded lattice + jitter)",
@@ -504,12 +512,15 @@ def run_ours(args, sc, cfg, corr):
     solver.close()
     if rank == 0:
         line = {
-            "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
+            "metric": WORKLOADS[args.workload][0], "value": round(value, 2), "unit": UNIT,
+            "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded lattice block + uniform jitter 0.01h)",
-            "config": {"workload": args.workload, "particles": sc.n, "block": [100, 100, 100],
-                       "box_block_widths": [3.0, 1.5, 1.5], "dt": sc.dt, "solver_iterations": 4,
+            "config": {"workload": args.workload, "particles": sc.n,
+                       "block": WORKLOADS[args.workload][1],
+                       "box_block_widths": WORKLOADS[args.workload][2], "dt": sc.dt,
+                       "solver_iterations": 4,
                        "max_neighbours": cfg.maxNeighbours, "table_size": table_size,
                        "corr": {"k": corr.k, "n": corr.n, "delta_q": corr.delta_q},
                        "math": "exact" if args.exact else "fast",
