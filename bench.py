@@ -101,6 +101,9 @@ def dist_env():
     return e.world, e.rank, e.local_rank
 
 
+FP32_PEAK_TFLOPS = round(152 * 128 * 2 * 2.07e9 / 1e12, 1)  # nominal, no FP32 peak is measured
+
+
 def load_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -480,6 +483,21 @@ def run_ours(args, sc, cfg, corr):
                 "step_algorithmic_bytes": int(step_bytes),
                 "step_achieved": round(step_bytes / (ms / args.steps / 1000.0) / 1e9, 1)}
 
+    # secondary figure: the step's FP32 arithmetic (counted by ncu per kernel, per particle) against
+    # the nominal FP32 rate
+    fp32 = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "fp32_ops_%s.json" % args.workload)) as f:
+            fo = json.load(f)
+        flops_step = float(fo["flops_per_particle_step"]) * sc.n
+        tf = flops_step / (ms / args.steps / 1000.0) / 1e12
+        fp32 = {"flops_per_step": int(flops_step), "achieved_tflops": round(tf, 2),
+                "peak_tflops": FP32_PEAK_TFLOPS, "frac": round(tf / FP32_PEAK_TFLOPS, 4),
+                "peak_source": "nominal: 152 SMs x 128 FP32 lanes x 2 flops x 2.07 GHz",
+                "counts": "profiles/fp32_ops_%s.json" % args.workload}
+    except Exception:
+        pass
+
     # end to end through the public API: pinned host records -> device, step, -> host
     e2e = None
     if not args.no_e2e:
@@ -531,6 +549,7 @@ def run_ours(args, sc, cfg, corr):
                        "pair_blocks_autotuned": pair_blocks,
                        "buckets_per_particle": round(buckets_per_particle, 4)},
             "roofline": roofline,
+            "fp32": fp32,
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": launches_per_step * args.steps,
