@@ -216,6 +216,23 @@ def test_zero_iterations_bitexact():
     assert_records_bitexact(g, o)
 
 
+@pytest.mark.parametrize("opts", [0, ak.OPT_EXACT_MATH], ids=["fast", "exact"])
+def test_interior_lattice_density_known_answer(opts):
+    """The centre of a resting lattice at spacing h/2 has 26 neighbours and density
+    W(0) + 6 W(h/2) + 12 W(h/sqrt 2) + 8 W(h sqrt 3/2) = 8082.3 (computed in float64)."""
+    from test_oracle import lattice_density_known_answer, lattice_kat_scene
+
+    p, cfg, centre = lattice_kat_scene()
+    sc = scene.Scene(p, (0.0, 0.0, 0.0), (3.0, 3.0, 3.0), 0.0083, "lattice_kat")
+    g, ge = run_gpu(sc, cfg, LambdaCorrParams(), 1, opts)
+    k = int(np.nonzero(ge["order"] == centre)[0][0])
+    assert ge["cnt"][k] == 26
+    assert float(g["density"][k]) == pytest.approx(lattice_density_known_answer(), rel=2e-5)
+    if opts:
+        o, _ = run_oracle(sc, cfg, LambdaCorrParams(), 1)
+        assert_records_bitexact(g, o)
+
+
 @pytest.mark.parametrize("n", [1, 2, 7])
 def test_tiny_particle_counts(n):
     sc = scene.dam_break((30, 30, 30), seed=1)

@@ -69,6 +69,35 @@ def test_poly6_known_answer():
     assert oracle.poly6(0.0100001, 0.1) == 0.0
 
 
+def lattice_density_known_answer(h=0.1):
+    """Density of an interior particle of a lattice at spacing h/2 (mass 1), in float64: W(0) plus
+    the 26 neighbours closer than h (6 at h/2, 12 at h/sqrt(2), 8 at h sqrt(3)/2; the 6 at exactly h
+    are not neighbours), with poly6's 315 / (64 * 3.14 * h^9)."""
+    k = 315.0 / (64.0 * 3.14 * h ** 9)
+    w = lambda r2: k * (h * h - r2) ** 3
+    q = (h / 2) ** 2
+    return w(0.0) + 6 * w(q) + 12 * w(2 * q) + 8 * w(3 * q)
+
+
+def lattice_kat_scene():
+    """A 7^3 lattice at spacing 0.05 = h/2, at rest, with no gravity, away from the walls."""
+    p = scene.lattice_block((7, 7, 7), 0.05, (1.0, 1.0, 1.0))
+    cfg = PBFConfig(gravity=(0.0, 0.0, 0.0), solverIterations=1)
+    return p, cfg, 3 * 49 + 3 * 7 + 3  # the centre particle's index
+
+
+def test_interior_lattice_density_known_answer():
+    want = lattice_density_known_answer()
+    assert want == pytest.approx(8082.3, abs=0.05)
+    p, cfg, centre = lattice_kat_scene()
+    P = oracle.make_params(cfg, LambdaCorrParams(), 0.0083, (0.0, 0.0, 0.0), (3.0, 3.0, 3.0),
+                           n=p.shape[0], flags=oracle.FMA)
+    perm, nbr, cnt = oracle.step(p, P, want_lists=True)
+    k = int(np.nonzero(perm == centre)[0][0])
+    assert cnt[k] == 26
+    assert float(p["density"][k]) == pytest.approx(want, rel=2e-6)
+
+
 def test_hash_known_answers():
     """NeighbourSearchCUDA.cu:23-27 restated with Python integers."""
     def ref(cx, cy, cz, t):
