@@ -102,3 +102,29 @@ def test_two_gloo_ranks_equal_global(oracle_mod):
         assert p.exitcode == 0
     for _, b in res:
         assert b == glob.tobytes()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("world", [2, 3])
+def test_decomposed_steps_on_the_cuda_solver_equal_global(cuda_lib, world):
+    """Each slab stepped by the CUDA solver (exact math, the whole scene's table size), one slab
+    after another on one GPU: the reassembled records equal the single-domain CUDA step's, byte
+    for byte, over three steps."""
+    import akuaengine_gb300 as ak
+    from akuaengine_gb300 import PBFSolver
+
+    sc = _scene()
+    cfg, corr = scene.benchmark_params()
+    table = cfg.maxNeighbours * sc.n
+
+    def local_step(rec):
+        with PBFSolver(rec.shape[0], cfg, corr, options=ak.OPT_EXACT_MATH, table_size=table) as s:
+            s.step_host(rec, sc.dt, sc.box_min, sc.box_max)
+
+    glob = sc.particles.copy()
+    dec = sc.particles.copy()
+    with PBFSolver(sc.n, cfg, corr, options=ak.OPT_EXACT_MATH) as s:
+        for _ in range(3):
+            s.step_host(glob, sc.dt, sc.box_min, sc.box_max)
+            dec = slabs.decomposed_step(dec, world, cfg, sc.dt, local_step)
+            assert dec.tobytes() == glob.tobytes()
