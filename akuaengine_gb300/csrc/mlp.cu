@@ -57,7 +57,8 @@ int enqueue_forward(const akua_mlp* m, const float* feat, int n, float* out, flo
                     float* out4, cudaStream_t st) {
     const int tiles = (n + kTile - 1) / kTile;
     const int grid = std::max(1, std::min(tiles, 5 * m->sms));  // 5 x 40 KB of shared memory
-    k_mlp_forward<<<grid, kThreads, 0, st>>>(m->params, m->norm, feat, n, out, out2, out4, m->err);
+    k_mlp_forward<<<grid, kThreads, 0, st>>>(m->params, m->image, m->norm, feat, n, out, out2,
+                                             out4, m->err);
     return status_of(cudaGetLastError());
 }
 }  // namespace akua::mlp
@@ -79,6 +80,8 @@ int akua_mlp_create(akua_mlp** out) {
     if (e == cudaSuccess) e = cudaMalloc(&m->v, pb);
     if (e == cudaSuccess) e = cudaMalloc(&m->norm, sizeof(float) * akua::mlp::kNorm);
     if (e == cudaSuccess) e = cudaMalloc(&m->err, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&m->image, akua::mlp::kImageBytes);
+    if (e == cudaSuccess) e = cudaMemset(m->image, 0, akua::mlp::kImageBytes);  // zero weights
     if (e == cudaSuccess) e = cudaMemset(m->params, 0, pb);
     if (e == cudaSuccess) e = cudaMemset(m->grad, 0, pb + sizeof(float));
     if (e == cudaSuccess) e = cudaMemset(m->m, 0, pb);
@@ -107,7 +110,7 @@ int akua_mlp_destroy(akua_mlp* m) {
     Guard g(m->device);
     cudaDeviceSynchronize();
     for (void* p : {(void*)m->params, (void*)m->grad, (void*)m->m, (void*)m->v, (void*)m->norm,
-                    (void*)m->err})
+                    (void*)m->err, (void*)m->image})
         if (p) cudaFree(p);
     delete m;
     return AKUA_OK;
@@ -121,6 +124,11 @@ int akua_mlp_set_params(akua_mlp* m, const float* host, int32_t count) {
     const size_t pb = sizeof(float) * akua::mlp::kParams;
     cudaError_t e = cudaDeviceSynchronize();
     if (e == cudaSuccess) e = cudaMemcpy(m->params, host, pb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        akua::mlp::k_mlp_image<<<1, akua::mlp::kThreads>>>(m->params, m->image);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e == cudaSuccess) e = cudaMemset(m->m, 0, pb);
     if (e == cudaSuccess) e = cudaMemset(m->v, 0, pb);
     if (e == cudaSuccess) e = cudaMemset(m->grad, 0, pb + sizeof(float));
@@ -194,7 +202,12 @@ int akua_mlp_adam_step(akua_mlp* m, const float* features, const float* targets,
     const int blocks = (akua::mlp::kParams + 1 + 255) / 256;
     akua::mlp::k_mlp_adam<<<blocks, 256, 0, st>>>(m->params, m->grad, m->m, m->v, learningRate,
                                                  b1, b2, 1e-8f, bc1, bc2);
-    return status_of(cudaGetLastError());
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) {  // the forward pass reads the updated weights from their image
+        akua::mlp::k_mlp_image<<<1, akua::mlp::kThreads, 0, st>>>(m->params, m->image);
+        e = cudaGetLastError();
+    }
+    return status_of(e);
 }
 
 int akua_mlp_synchronize(akua_mlp* m, void* stream) {

@@ -21,8 +21,11 @@
 // of D is the bias gradient.
 #pragma once
 
+#include <cstddef>
 #include <cstdint>
+#include <cstring>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "tc05.cuh"
@@ -60,6 +63,19 @@ __device__ __forceinline__ float tanh_hw(float x) {
 }
 __device__ __forceinline__ float sigmoid(float z) { return __fmaf_rn(0.5f, tanh_hw(0.5f * z), 0.5f); }
 __device__ __forceinline__ float silu(float z) { return z * sigmoid(z); }
+// Inference: silu of two values, the tanh evaluated on an FP16 pair (tanh.approx.f16x2: one
+// multi-function operation for two activations; its error, about 2^-11 relative, is below the
+// BF16 rounding the hidden activations get next).
+__device__ __forceinline__ float2 silu2(float z0, float z1) {
+    const __half2 hz = __floats2half2_rn(0.5f * z0, 0.5f * z1);
+    uint32_t in, out;
+    memcpy(&in, &hz, 4);
+    asm("tanh.approx.f16x2 %0, %1;" : "=r"(out) : "r"(in));
+    __half2 ht;
+    memcpy(&ht, &out, 4);
+    const float2 t = __half22float2(ht);
+    return make_float2(z0 * __fmaf_rn(0.5f, t.x, 0.5f), z1 * __fmaf_rn(0.5f, t.y, 0.5f));
+}
 __device__ __forceinline__ float dsilu(float z) {
     const float s = sigmoid(z);
     return s * (1.0f + z * (1.0f - s));
@@ -112,6 +128,18 @@ __device__ __forceinline__ void stage_weight(uint8_t* dst, const float* __restri
     }
 }
 
+// BF16 operand images of W1, W2, W3 in the forward pass's shared-memory layout, rebuilt by
+// k_mlp_image whenever the parameters change; a forward CTA copies them instead of converting.
+constexpr int kImageBytes = (kHid * kInPad + 2 * kHid * kHid) * 2;
+
+__global__ void __launch_bounds__(kThreads)
+    k_mlp_image(const float* __restrict__ params, uint8_t* __restrict__ image) {
+    const int t = threadIdx.x;
+    stage_weight(image, params + kW1, kIn, kInPad, false, t);
+    stage_weight(image + kHid * kInPad * 2, params + kW2, kHid, kHid, false, t);
+    stage_weight(image + kHid * kInPad * 2 + kHid * kHid * 2, params + kW3, kHid, kHid, false, t);
+}
+
 // ------------------------------------------------------------------------------------ forward
 struct FwdSmem {
     alignas(128) uint8_t w1[kHid * kInPad * 2];
@@ -139,7 +167,12 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t taddr, const float* b, 
     for (int c = 0; c < 4; ++c) {
         float v[16];
 #pragma unroll
-        for (int q = 0; q < 16; ++q) v[q] = silu(__uint_as_float(r[c][q]) + b[16 * c + q]);
+        for (int q = 0; q < 16; q += 2) {
+            const float2 a = silu2(__uint_as_float(r[c][q]) + b[16 * c + q],
+                                   __uint_as_float(r[c][q + 1]) + b[16 * c + q + 1]);
+            v[q] = a.x;
+            v[q + 1] = a.y;
+        }
         store_row64(h, t, v, 16 * c);
     }
 }
@@ -157,8 +190,12 @@ __device__ __forceinline__ float output_layer(uint32_t taddr, const float* b3, c
 #pragma unroll
     for (int c = 0; c < 4; ++c)
 #pragma unroll
-        for (int q = 0; q < 16; ++q)
-            y = __fmaf_rn(w4[16 * c + q], silu(__uint_as_float(r[c][q]) + b3[16 * c + q]), y);
+        for (int q = 0; q < 16; q += 2) {
+            const float2 a = silu2(__uint_as_float(r[c][q]) + b3[16 * c + q],
+                                   __uint_as_float(r[c][q + 1]) + b3[16 * c + q + 1]);
+            y = __fmaf_rn(w4[16 * c + q], a.x, y);
+            y = __fmaf_rn(w4[16 * c + q + 1], a.y, y);
+        }
     return y;
 }
 
@@ -179,14 +216,21 @@ __device__ __forceinline__ void load_features(const float* __restrict__ feat, in
 // out[i] = lambda0_i + blend * (p_i - lambda0_i), lambda0 = feature 3 (blend 1: out = p); the
 // latter also into out4[4 i] when given.
 __global__ void __launch_bounds__(kThreads)
-    k_mlp_forward(const float* __restrict__ params, const float* __restrict__ norm,
-                  const float* __restrict__ feat, int n, float* __restrict__ out,
-                  float* __restrict__ out2, float* __restrict__ out4, uint32_t* __restrict__ err) {
+    k_mlp_forward(const float* __restrict__ params, const uint8_t* __restrict__ image,
+                  const float* __restrict__ norm, const float* __restrict__ feat, int n,
+                  float* __restrict__ out, float* __restrict__ out2, float* __restrict__ out4,
+                  uint32_t* __restrict__ err) {
     __shared__ FwdSmem S;
+    static_assert(offsetof(FwdSmem, w2) == offsetof(FwdSmem, w1) + sizeof(S.w1) &&
+                      offsetof(FwdSmem, w3) == offsetof(FwdSmem, w2) + sizeof(S.w2) &&
+                      sizeof(S.w1) + sizeof(S.w2) + sizeof(S.w3) == kImageBytes,
+                  "the weight image is w1, w2, w3 back to back");
     const int t = threadIdx.x, warp = t >> 5;
-    stage_weight(S.w1, params + kW1, kIn, kInPad, false, t);
-    stage_weight(S.w2, params + kW2, kHid, kHid, false, t);
-    stage_weight(S.w3, params + kW3, kHid, kHid, false, t);
+    {
+        const uint4* src = reinterpret_cast<const uint4*>(image);
+        uint4* dst = reinterpret_cast<uint4*>(S.w1);
+        for (int k = t; k < kImageBytes / 16; k += kThreads) dst[k] = __ldg(src + k);
+    }
     if (t < kHid) {
         S.b1[t] = params[kB1 + t];
         S.b2[t] = params[kB2 + t];

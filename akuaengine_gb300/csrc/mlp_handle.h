@@ -8,6 +8,7 @@ struct akua_mlp {
     int device = 0;
     int sms = 0;
     float* params = nullptr;  // FP32 master parameters [kParams]
+    uint8_t* image = nullptr; // BF16 operand images of W1..W3 for the forward pass
     float* grad = nullptr;    // [kParams] gradient, then the loss
     float* m = nullptr;       // Adam moments
     float* v = nullptr;
