@@ -101,7 +101,8 @@ def dist_env():
     return e.world, e.rank, e.local_rank
 
 
-FP32_PEAK_TFLOPS = round(152 * 128 * 2 * 2.07e9 / 1e12, 1)  # nominal, no FP32 peak is measured
+SM_COUNT = 152
+FP32_PEAK_TFLOPS = round(SM_COUNT * 128 * 2 * 2.07e9 / 1e12, 1)  # nominal: no FP32 peak is measured
 
 
 def load_peaks():
@@ -475,11 +476,25 @@ def run_ours(args, sc, cfg, corr):
         traffic = tr["bytes_per_launch"].get(dom)
     except Exception:
         pass
+    # the walk is bound by instruction issue: its warp instructions per launch (ncu) over the
+    # event-timed duration, against one instruction per scheduler per clock (4 per SM)
+    issue = None
+    try:
+        inst = float(tr["warp_instructions_per_launch"][dom])
+        mhz = float(clocks.get("sm_mhz") or 2070.0)
+        peak_ips = SM_COUNT * 4 * mhz * 1e6
+        issue = {"warp_instructions": int(inst), "achieved_per_s": round(inst / per_launch_s, 1),
+                 "peak_per_s": round(peak_ips, 1), "frac": round(inst / per_launch_s / peak_ips, 4),
+                 "source": "profiles/traffic_%s.json (ncu smsp__inst_executed.sum); peak at the "
+                           "sampled SM clock" % args.workload}
+    except Exception:
+        pass
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
                 "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                 "traffic": traffic, "algorithmic_bytes": int(alg_bytes),
                 "peak_source": "measured hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured"
                 else "fallback 6.8 TB/s",
+                "issue": issue,
                 "step_algorithmic_bytes": int(step_bytes),
                 "step_achieved": round(step_bytes / (ms / args.steps / 1000.0) / 1e9, 1)}
 
