@@ -173,15 +173,6 @@ __global__ void __launch_bounds__(kElemBlock)
     bval[r] = (uint32_t)i;
 }
 
-// The new reference rank of every particle, by import index (the inverse of the hash sort's
-// permutation), for the gather.
-__global__ void __launch_bounds__(kElemBlock)
-    k_rank_scatter(const StepParams* __restrict__ P, const uint32_t* __restrict__ refperm,
-                   uint32_t* __restrict__ rank_of_import) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= P->n) return;
-    rank_of_import[refperm[r]] = (uint32_t)r;
-}
 
 // Moves the state into the new internal order (slot s holds the particle of import index
 // sp_import[s], reference rank rank_of_import[...]) and writes the predicted positions, both maps
@@ -242,7 +233,7 @@ __global__ void __launch_bounds__(kElemBlock)
 // The bucket table (NeighbourSearchCUDA.cu:52-65 builds hash -> first sorted index).  Here an
 // entry is (x, y): y = 0 for a hash no particle carries; otherwise y = bucket length and x = the
 // bucket's first internal slot, or, with bit 31 of y set (a mixed bucket, see k_table_build), its
-// first reference rank.  The table is all-empty between steps: k_table_clear empties this step's
+// first reference rank.  The table is all-empty between steps: k_xsph empties this step's
 // entries after the walk.
 
 // One thread per bucket start (the first reference rank carrying a hash) reads its bucket's ranks
@@ -271,15 +262,6 @@ __global__ void __launch_bounds__(kElemBlock)
     table[k] = run ? make_uint2(s0, len) : make_uint2((uint32_t)r, len | kMixedBucket);
 }
 
-// Empties this step's entries, leaving the table all-empty for the next step.
-__global__ void __launch_bounds__(kElemBlock)
-    k_table_clear(const StepParams* __restrict__ P, const uint32_t* __restrict__ kr,
-                  uint2* __restrict__ table) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= P->n) return;
-    const uint32_t k = kr[r];
-    if (r == 0 || kr[r - 1] != k) table[k] = make_uint2(0u, 0u);
-}
 
 // Writes every field of every particle into the attached records in reference order (record r
 // holds the particle of reference rank r), staged through shared memory so global writes are

@@ -503,13 +503,17 @@ __global__ void __launch_bounds__(kMaxPairBlock)
 }
 
 // XSPH viscosity (IntegrationCUDA.cu:167-195) from the confined-velocity snapshot in the records
-// (x, m / rho | v).
+// (x, m / rho | v).  Also leaves the bucket table all-empty for the next step.
 __global__ void __launch_bounds__(kMaxPairBlock)
     k_xsph(const StepParams* __restrict__ P, const float4* __restrict__ xv8,
            const uint4* __restrict__ nbr4, const uint32_t* __restrict__ cnt,
-           float4* __restrict__ v4) {
+           float4* __restrict__ v4, const uint32_t* __restrict__ kr, uint2* __restrict__ table) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P->n) return;
+    {  // the walk is done: empty this step's bucket entries (thread i: the bucket starting at rank i)
+        const uint32_t k = kr[i];
+        if (i == 0 || kr[i - 1] != k) table[k] = make_uint2(0u, 0u);
+    }
     const StepParams& p = params_for(P, i);
     const int n = p.n;
     if (i >= n) return;

@@ -330,9 +330,6 @@ void enqueue_pairs(akua_pbf* s, cudaStream_t st, Marker& mark) {
         akua::mlp::enqueue_forward(s->warm, s->feat, n, s->lam, s->lacc, &s->psl->w, st);
         mark("k_mlp_forward");
     }
-    akua::k_table_clear<<<grid_for(n, akua::kElemBlock), akua::kElemBlock, 0, st>>>(s->d_params,
-                                                                                   s->kr, s->table);
-    mark("k_table_clear");
     for (int it = 0; it < iters; ++it) {
         float4* cur = ps[it & 1];
         float4* nxt = ps[(it + 1) & 1];
@@ -369,7 +366,8 @@ void enqueue_pairs(akua_pbf* s, cudaStream_t st, Marker& mark) {
                                                     s->rho, nbr4, s->cnt, s->xv8, s->psl,
                                                     s->mass_bits);
     mark("k_confine");
-    akua::k_xsph<<<gp(5), pb[5], 0, st>>>(s->d_params, s->xv8, nbr4, s->cnt, s->v4);
+    akua::k_xsph<<<gp(5), pb[5], 0, st>>>(s->d_params, s->xv8, nbr4, s->cnt, s->v4,
+                                          s->kr, s->table);
     mark("k_xsph");
 }
 
@@ -398,10 +396,9 @@ void enqueue_body(akua_pbf* s, cudaStream_t st, const char* aos, size_t stride, 
     akua::radix::sort_pairs(sb, s->plan_sp, s->kb0, s->vb0, s->kb1, s->vb1, false,
                             s->sort_scratch_b, n, &dummy, &s->spperm, fork ? mark_b : mark);
     if (fork) cudaEventRecord(s->ev_join, sb);
+    // the last pass also writes each import slot's reference rank (the inverse permutation)
     akua::radix::sort_pairs(st, s->plan_ref, s->ka0, s->va0, s->ka1, s->va1, false,
-                            s->sort_scratch, n, &s->kr, &s->refperm, mark);
-    akua::k_rank_scatter<<<ge, akua::kElemBlock, 0, st>>>(s->d_params, s->refperm, s->rank_of_import);
-    mark("k_rank_scatter");
+                            s->sort_scratch, n, &s->kr, &s->refperm, mark, s->rank_of_import);
     if (fork) {
         cudaStreamWaitEvent(st, s->ev_join, 0);
         mark.launches += mark_b.launches;

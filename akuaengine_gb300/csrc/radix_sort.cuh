@@ -130,12 +130,13 @@ __global__ void __launch_bounds__(SCAN_BLOCK) scan_rows(uint32_t* __restrict__ c
     }
 }
 
-// Stable scatter of one tile.  `vals_in == nullptr` means the payload is the key's index.
+// Stable scatter of one tile.  `vals_in == nullptr` means the payload is the key's index.  With
+// `rank_out`, rank_out[payload] = the pair's output position too (the inverse permutation).
 template <int BITS>
 __global__ void __launch_bounds__(BLOCK)
     downsweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
               uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, int n, int shift,
-              const uint32_t* __restrict__ offsets, int tiles) {
+              const uint32_t* __restrict__ offsets, int tiles, uint32_t* __restrict__ rank_out) {
     constexpr int RADIX = 1 << BITS;
     extern __shared__ uint32_t wbase_flat[];  // [WARPS][RADIX]
     uint32_t(*wbase)[RADIX] = reinterpret_cast<uint32_t(*)[RADIX]>(wbase_flat);
@@ -185,6 +186,7 @@ __global__ void __launch_bounds__(BLOCK)
             const uint32_t dst = wbase[warp][d] + rank[r];
             keys_out[dst] = key[r];
             vals_out[dst] = val[r];
+            if (rank_out) rank_out[val[r]] = dst;
         }
     }
 }
@@ -192,15 +194,15 @@ __global__ void __launch_bounds__(BLOCK)
 template <int BITS, class Mark>
 inline void run_pass(cudaStream_t s, const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
                      uint32_t* vout, uint32_t* counts, uint32_t* totals, int n, int shift,
-                     Mark& mark) {
+                     uint32_t* rank_out, Mark& mark) {
     const int tiles = num_tiles(n);
     constexpr int RADIX = 1 << BITS;
     upsweep<BITS><<<tiles, BLOCK, 0, s>>>(kin, n, shift, counts, totals, tiles);
     mark("radix_upsweep");
     scan_rows<<<RADIX, SCAN_BLOCK, 0, s>>>(counts, totals, tiles);
     mark("radix_scan");
-    downsweep<BITS><<<tiles, BLOCK, WARPS * RADIX * sizeof(uint32_t), s>>>(kin, vin, kout, vout, n,
-                                                                           shift, counts, tiles);
+    downsweep<BITS><<<tiles, BLOCK, WARPS * RADIX * sizeof(uint32_t), s>>>(
+        kin, vin, kout, vout, n, shift, counts, tiles, rank_out);
     mark("radix_downsweep");
 }
 
@@ -211,11 +213,13 @@ inline size_t scratch_words(int n) {
 
 // Sorts (k0, v0) by the low plan bits, ping-ponging with (k1, v1); all four buffers hold n words.
 // With `index_payload` the input payload is each key's index and v0 is not read.  The result
-// buffers are returned through keys_out / vals_out.  `mark(name)` is called after every kernel.
+// buffers are returned through keys_out / vals_out.  With `rank_out` (n words), the last pass
+// also writes rank_out[payload] = output position.  `mark(name)` is called after every kernel.
 template <class Mark>
 inline void sort_pairs(cudaStream_t s, const Plan& plan, uint32_t* k0, uint32_t* v0, uint32_t* k1,
                        uint32_t* v1, bool index_payload, uint32_t* scratch, int n,
-                       uint32_t** keys_out, uint32_t** vals_out, Mark& mark) {
+                       uint32_t** keys_out, uint32_t** vals_out, Mark& mark,
+                       uint32_t* rank_out = nullptr) {
     uint32_t* counts = scratch;
     uint32_t* totals = scratch + (size_t)MAX_RADIX * num_tiles(n);
     cudaMemsetAsync(totals, 0, sizeof(uint32_t) * MAX_PASSES * MAX_RADIX, s);
@@ -225,14 +229,15 @@ inline void sort_pairs(cudaStream_t s, const Plan& plan, uint32_t* k0, uint32_t*
     uint32_t* vout = v1;
     for (int p = 0; p < plan.passes; ++p) {
         uint32_t* tot = totals + (size_t)p * MAX_RADIX;
+        const bool last = p + 1 == plan.passes;
         // a digit narrower than 8 bits only occurs in the last pass, where the key's higher
         // bits are zero, so the 8-bit kernel sorts it correctly
         if (plan.width[p] <= 8)
-            run_pass<8>(s, kin, vin, kout, vout, counts, tot, n, plan.shift[p], mark);
+            run_pass<8>(s, kin, vin, kout, vout, counts, tot, n, plan.shift[p], last ? rank_out : nullptr, mark);
         else if (plan.width[p] == 9)
-            run_pass<9>(s, kin, vin, kout, vout, counts, tot, n, plan.shift[p], mark);
+            run_pass<9>(s, kin, vin, kout, vout, counts, tot, n, plan.shift[p], last ? rank_out : nullptr, mark);
         else
-            run_pass<10>(s, kin, vin, kout, vout, counts, tot, n, plan.shift[p], mark);
+            run_pass<10>(s, kin, vin, kout, vout, counts, tot, n, plan.shift[p], last ? rank_out : nullptr, mark);
         if (kout == k1) {
             kin = k1; vin = v1; kout = k0; vout = v0;
         } else {

@@ -99,11 +99,14 @@ extern "C" int akua_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* 
         uint32_t* vout = to_out ? vals_out : tmp_vals;
         uint32_t* tot = totals + (size_t)p * akua::radix::MAX_RADIX;
         if (plan.width[p] <= 8)
-            akua::radix::run_pass<8>(st, kin, vin, kout, vout, counts, tot, n, plan.shift[p], mark);
+            akua::radix::run_pass<8>(st, kin, vin, kout, vout, counts, tot, n, plan.shift[p],
+                                      nullptr, mark);
         else if (plan.width[p] == 9)
-            akua::radix::run_pass<9>(st, kin, vin, kout, vout, counts, tot, n, plan.shift[p], mark);
+            akua::radix::run_pass<9>(st, kin, vin, kout, vout, counts, tot, n, plan.shift[p],
+                                      nullptr, mark);
         else
-            akua::radix::run_pass<10>(st, kin, vin, kout, vout, counts, tot, n, plan.shift[p], mark);
+            akua::radix::run_pass<10>(st, kin, vin, kout, vout, counts, tot, n, plan.shift[p],
+                                      nullptr, mark);
         kin = kout;
         vin = vout;
     }

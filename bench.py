@@ -53,14 +53,12 @@ KERNEL_BYTES = {
     "k_keys": lambda L, B: 16 + 16 + 4 + 12,
     "radix_upsweep": lambda L, B: 4,                  # R key (per pass)
     "radix_downsweep": lambda L, B: 16,               # R key, value; W key, value (per pass)
-    "k_rank_scatter": lambda L, B: 8,                 # R reference permutation; W slot rank
     # R two permutations, x|m, v, colour, size, old rank; W x|m, colour, size, x*|m, rank->slot,
     # slot->rank, reference-ordered x*|m, order
     "k_gather": lambda L, B: 8 + 16 + 16 + 16 + 4 + 4 + 16 + 16 + 4 + 16 + 4 + 4 + 16 + 4,
     "k_table_build": lambda L, B: 4 + 4 + 8 * B,      # R keys, slots; W entry
     # R x*|m, 27 bucket entries per cell run; W lists, count, rho, lambda, x*|lambda
     "k_search": lambda L, B: 16 + 27 * 8 * B + L + 4 + 8 + 16,
-    "k_table_clear": lambda L, B: 4 + 8 * B,          # R keys; W entry
     # R x*|m, count, lists; W rho, lambda, x*|lambda
     "k_density_lambda": lambda L, B: 16 + 4 + L + 8 + 16,
     # R x*|m, lambda, count, lists; W x*|m, delta
@@ -71,7 +69,8 @@ KERNEL_BYTES = {
     "k_vorticity": lambda L, B: 16 + 16 + 4 + L + 16 + 16,   # R x, v, count, lists; W omega, x|omega
     # R x, v, omega, rho, count, lists; W record (x|m/rho, v)
     "k_confine": lambda L, B: 16 + 16 + 16 + 4 + 4 + L + 32,
-    "k_xsph": lambda L, B: 32 + 4 + L + 16,                  # R record, count, lists; W v
+    # R record, count, lists, keys; W v, emptied bucket entries
+    "k_xsph": lambda L, B: 32 + 4 + L + 16 + 4 + 8 * B,
     # R slot, key, x, v, v*, delta, omega, colour, rho, lambda, size; W record 108
     "k_export": lambda L, B: 4 + 4 + 16 * 6 + 4 + 4 + 4 + 108,
 }
