@@ -85,43 +85,6 @@ __global__ void k_set_params_chunk(ParamChunk c, StepParams* __restrict__ dst) {
     if (blockIdx.x == 0 && threadIdx.x < c.count) dst[threadIdx.x] = c.p[threadIdx.x];
 }
 
-// Reads the attached records (buffer order = previous reference order) into the state.  A block
-// stages its records through shared memory so global reads are coalesced when records are packed.
-// With `carry`, density, lambda and position_delta are read too: with zero solver iterations the
-// reference leaves them as they were.
-__global__ void __launch_bounds__(kIoBlock)
-    k_import(const char* __restrict__ aos, uint64_t stride, int n, float4* __restrict__ x4,
-             float4* __restrict__ v4, float4* __restrict__ col4, float* __restrict__ size,
-             uint32_t* __restrict__ rref, float* __restrict__ rho, float* __restrict__ lam,
-             float4* __restrict__ dp4, int carry) {
-    __shared__ __align__(16) float rec[kIoBlock * kRecWords];
-    const int r0 = blockIdx.x * kIoBlock;
-    const int cnt = min(kIoBlock, n - r0);
-    if (stride == kRecWords * 4) {
-        const float* src = reinterpret_cast<const float*>(aos) + (size_t)r0 * kRecWords;
-        copy_words(rec, src, cnt * kRecWords);
-    } else {
-        for (int w = threadIdx.x; w < cnt * kRecWords; w += kIoBlock) {
-            const int q = w / kRecWords, f = w - q * kRecWords;
-            rec[w] = reinterpret_cast<const float*>(aos + (uint64_t)(r0 + q) * stride)[f];
-        }
-    }
-    __syncthreads();
-    const int t = threadIdx.x;
-    if (t >= cnt) return;
-    const int i = r0 + t;
-    const float* r = rec + t * kRecWords;
-    x4[i] = make_float4(r[kPos], r[kPos + 1], r[kPos + 2], r[kMass]);
-    v4[i] = make_float4(r[kVel], r[kVel + 1], r[kVel + 2], 0.f);
-    col4[i] = make_float4(r[kColor], r[kColor + 1], r[kColor + 2], r[kColor + 3]);
-    size[i] = r[kSize];
-    rref[i] = (uint32_t)i;
-    if (carry) {
-        rho[i] = r[kDensity];
-        lam[i] = r[kLambda];
-        dp4[i] = make_float4(r[kDelta], r[kDelta + 1], r[kDelta + 2], 0.f);
-    }
-}
 
 // Predicted position (IntegrationCUDA.cu:34-35): v* = fma(g, dt, v); x* = fma(v*, dt, x).
 __device__ __forceinline__ float3 predict(const StepParams& p, float4 x, float4 v) {
@@ -150,9 +113,25 @@ __device__ __forceinline__ uint32_t morton_key(const StepParams& p, int cx, int 
     return spread10(x) | (spread10(y) << 1) | (spread10(z) << 2);
 }
 
+// Hash key and Morton key of the predicted position of import slot i at previous reference rank r.
+__device__ __forceinline__ void write_keys(const StepParams& p, float4 x, float4 v, uint32_t r,
+                                           uint32_t i, uint32_t* __restrict__ akey,
+                                           uint32_t* __restrict__ aval, uint32_t* __restrict__ bkey,
+                                           uint32_t* __restrict__ bval) {
+    const float3 xs = predict(p, x, v);
+    const uint32_t h = cell_hash(cell_coord(xs.x, p.hash_cell), cell_coord(xs.y, p.hash_cell),
+                                 cell_coord(xs.z, p.hash_cell), p.table_size, p.table_magic);
+    akey[r] = p.table_offset + h;
+    aval[r] = i;
+    bkey[r] = ((uint32_t)p.scene << (3 * p.sp_bits)) |
+              morton_key(p, cell_coord(xs.x, p.search_cell), cell_coord(xs.y, p.search_cell),
+                         cell_coord(xs.z, p.search_cell));
+    bval[r] = i;
+}
+
 // Cell hash and Morton key of the walk cell of each predicted position, both scattered into the
 // previous reference order (so both stable sorts tie like the reference's), each with the import
-// index as payload.
+// index as payload.  Steps that import the records compute them in k_import instead.
 __global__ void __launch_bounds__(kElemBlock)
     k_keys(const StepParams* __restrict__ P, const float4* __restrict__ x4,
            const float4* __restrict__ v4, const uint32_t* __restrict__ rref,
@@ -160,17 +139,51 @@ __global__ void __launch_bounds__(kElemBlock)
            uint32_t* __restrict__ bval) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P->n) return;
-    const StepParams& p = params_for(P, i);
-    const float3 xs = predict(p, x4[i], v4[i]);
-    const uint32_t h = cell_hash(cell_coord(xs.x, p.hash_cell), cell_coord(xs.y, p.hash_cell),
-                                 cell_coord(xs.z, p.hash_cell), p.table_size, p.table_magic);
-    const uint32_t r = rref[i];
-    akey[r] = p.table_offset + h;
-    aval[r] = (uint32_t)i;
-    bkey[r] = ((uint32_t)p.scene << (3 * p.sp_bits)) |
-              morton_key(p, cell_coord(xs.x, p.search_cell), cell_coord(xs.y, p.search_cell),
-                         cell_coord(xs.z, p.search_cell));
-    bval[r] = (uint32_t)i;
+    write_keys(params_for(P, i), x4[i], v4[i], rref[i], (uint32_t)i, akey, aval, bkey, bval);
+}
+
+// Reads the attached records (buffer order = previous reference order) into the state, and writes
+// the sort keys as k_keys does (an import slot's previous reference rank is its index).  A block
+// stages its records through shared memory so global reads are coalesced when records are packed.
+// With `carry`, density, lambda and position_delta are read too: with zero solver iterations the
+// reference leaves them as they were.
+__global__ void __launch_bounds__(kIoBlock)
+    k_import(const StepParams* __restrict__ P, const char* __restrict__ aos, uint64_t stride,
+             int n, float4* __restrict__ x4, float4* __restrict__ v4, float4* __restrict__ col4,
+             float* __restrict__ size, uint32_t* __restrict__ rref, float* __restrict__ rho,
+             float* __restrict__ lam, float4* __restrict__ dp4, int carry,
+             uint32_t* __restrict__ akey, uint32_t* __restrict__ aval, uint32_t* __restrict__ bkey,
+             uint32_t* __restrict__ bval) {
+    __shared__ __align__(16) float rec[kIoBlock * kRecWords];
+    const int r0 = blockIdx.x * kIoBlock;
+    const int cnt = min(kIoBlock, n - r0);
+    if (stride == kRecWords * 4) {
+        const float* src = reinterpret_cast<const float*>(aos) + (size_t)r0 * kRecWords;
+        copy_words(rec, src, cnt * kRecWords);
+    } else {
+        for (int w = threadIdx.x; w < cnt * kRecWords; w += kIoBlock) {
+            const int q = w / kRecWords, f = w - q * kRecWords;
+            rec[w] = reinterpret_cast<const float*>(aos + (uint64_t)(r0 + q) * stride)[f];
+        }
+    }
+    __syncthreads();
+    const int t = threadIdx.x;
+    if (t >= cnt) return;
+    const int i = r0 + t;
+    const float* r = rec + t * kRecWords;
+    const float4 x = make_float4(r[kPos], r[kPos + 1], r[kPos + 2], r[kMass]);
+    const float4 v = make_float4(r[kVel], r[kVel + 1], r[kVel + 2], 0.f);
+    x4[i] = x;
+    v4[i] = v;
+    write_keys(params_for(P, i), x, v, (uint32_t)i, (uint32_t)i, akey, aval, bkey, bval);
+    col4[i] = make_float4(r[kColor], r[kColor + 1], r[kColor + 2], r[kColor + 3]);
+    size[i] = r[kSize];
+    rref[i] = (uint32_t)i;
+    if (carry) {
+        rho[i] = r[kDensity];
+        lam[i] = r[kLambda];
+        dp4[i] = make_float4(r[kDelta], r[kDelta + 1], r[kDelta + 2], 0.f);
+    }
 }
 
 

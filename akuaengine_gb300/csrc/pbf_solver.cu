@@ -377,9 +377,6 @@ void enqueue_body(akua_pbf* s, cudaStream_t st, const char* aos, size_t stride, 
     const int ge = grid_for(n, akua::kElemBlock);
     Marker mark{s, st, record};
     const bool carry = s->cfg.solverIterations == 0;
-    akua::k_keys<<<ge, akua::kElemBlock, 0, st>>>(s->d_params, s->x4, s->v4, s->rref, s->ka0,
-                                                  s->va0, s->kb0, s->vb0);
-    mark("k_keys");
     uint32_t* dummy = nullptr;
     // The two sorts are independent: reference order, stable by (hash, previous reference rank),
     // and internal order, stable by Morton cell over the previous reference order (payload: import
@@ -501,14 +498,19 @@ int do_step(akua_pbf* s, const char* aos, size_t stride, bool force_import, floa
     const bool import = force_import || !(s->options & AKUA_PBF_OPT_RESIDENT) || !s->state_valid;
     if (import) {
         akua::k_import<<<grid_for(s->n, akua::kIoBlock), akua::kIoBlock, 0, st>>>(
-            aos, stride, s->n, s->x4, s->v4, s->col4, s->size, s->rref, s->rho, s->lam, s->dp4,
-            s->cfg.solverIterations == 0 ? 1 : 0);
+            s->d_params, aos, stride, s->n, s->x4, s->v4, s->col4, s->size, s->rref, s->rho,
+            s->lam, s->dp4, s->cfg.solverIterations == 0 ? 1 : 0, s->ka0, s->va0, s->kb0, s->vb0);
         mark("k_import");
         if (learn_mode(s)) {  // the previous step's lambda sums, in the records' order
             cudaError_t ce = cudaMemcpyAsync(s->lacc, s->lacc_ref, sizeof(float) * s->n,
                                              cudaMemcpyDeviceToDevice, st);
             if (ce != cudaSuccess) return cuda_status(ce);
         }
+    }
+    if (!import) {  // the state is already on the device: only the sort keys
+        akua::k_keys<<<grid_for(s->n, akua::kElemBlock), akua::kElemBlock, 0, st>>>(
+            s->d_params, s->x4, s->v4, s->rref, s->ka0, s->va0, s->kb0, s->vb0);
+        mark("k_keys");
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_status(e);
@@ -937,11 +939,10 @@ int akua_pbf_read_debug(akua_pbf* s, int32_t what, void* dst, size_t bytes) {
 int akua_pbf_kernels_per_step(akua_pbf* s) {
     if (!s) return AKUA_ERR_INVALID_ARGUMENT;
     if (s->body_launches == 0) return AKUA_ERR_INVALID_ARGUMENT;  // no step issued yet
-    // parameter upload (one launch per chunk of scenes) + import (when it runs) + the body
-    const bool import = !(s->options & AKUA_PBF_OPT_RESIDENT);
+    // parameter upload (one launch per chunk of scenes) + import or the sort keys + the body
     const int uploads =
         s->scenes.empty() ? 1 : (int)((s->scenes.size() + akua::kParamChunk - 1) / akua::kParamChunk);
-    return uploads + (import ? 1 : 0) + s->body_launches;
+    return uploads + 1 + s->body_launches;
 }
 
 int akua_pbf_profile_begin(akua_pbf* s, int32_t max_steps) {

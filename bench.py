@@ -47,10 +47,10 @@ WORKLOAD = "dam_break_1m"
 # the mean bytes of one particle's list tiles (16 * ceil(count / 4)), `B` the mean number of bucket
 # table entries per particle (one 8-byte entry per occupied bucket), both taken from the run.
 KERNEL_BYTES = {
-    # R record 108; W x|m, v, colour, size, rank
-    "k_import": lambda L, B: 108 + 16 + 16 + 16 + 4 + 4,
+    # R record 108; W x|m, v, colour, size, rank, hash key and Morton key with their payloads
+    "k_import": lambda L, B: 108 + 16 + 16 + 16 + 4 + 4 + 16,
     # R x|m, v, rank; W hash key, index, Morton key
-    "k_keys": lambda L, B: 16 + 16 + 4 + 12,
+    "k_keys": lambda L, B: 16 + 16 + 4 + 16,
     "radix_upsweep": lambda L, B: 4,                  # R key (per pass)
     "radix_downsweep": lambda L, B: 16,               # R key, value; W key, value (per pass)
     # R two permutations, x|m, v, colour, size, old rank; W x|m, colour, size, x*|m, rank->slot,
