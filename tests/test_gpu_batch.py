@@ -88,3 +88,69 @@ def test_batch_rejects_single_scene_calls(cuda_lib):
     with pytest.raises(ak.AkuaError):
         bs.set_table_size(1000)
     bs.close()
+
+
+def _alone_with(b, k, cfg, corr, steps, opts, setup):
+    sc = b.scene(k)
+    c = dataclasses.replace(cfg, gravity=sc.meta["gravity"])
+    s = PBFSolver(sc.n, c, corr, options=opts)
+    setup(s)
+    p = sc.particles.copy()
+    for _ in range(steps):
+        s.step_host(p, sc.dt, sc.box_min, sc.box_max)
+    s.close()
+    return p
+
+
+def _batch_with(b, cfg, corr, steps, opts, setup):
+    import torch
+
+    bs = BatchSolver(b.scenes, cfg, corr, options=opts)
+    setup(bs)
+    buf = torch.from_numpy(b.particles.view(np.uint8).copy()).cuda()
+    for _ in range(steps):
+        bs.step(buf, b.dt)
+    got = buf.cpu().numpy().view(ak.PARTICLE_DTYPE)
+    bs.close()
+    return got
+
+
+@pytest.mark.gpu
+def test_batch_with_obstacles_equals_scenes_alone(cuda_lib):
+    """Obstacles set on a batch apply to every scene: each comes out as if stepped alone with them."""
+    b = scene.batched_dam_breaks(count=4, n_min=800, n_max=6000, seed=11)
+    cfg, corr = scene.benchmark_params()
+    shapes = [{"type": "sphere", "a": (0.25, 0.05, 0.25), "b": (0.0, 0.0, 0.0), "radius": 0.08},
+              {"type": "plane", "a": (0.0, 0.02, 0.0), "b": (0.0, 1.0, 0.0), "radius": 0.0}]
+    setup = lambda s: s.set_sdf_shapes(shapes)
+    steps = 5
+    got = _batch_with(b, cfg, corr, steps, ak.OPT_EXACT_MATH, setup)
+    for k, d in enumerate(b.scenes):
+        f, n = b.first[k], d["numParticles"]
+        want = _alone_with(b, k, cfg, corr, steps, ak.OPT_EXACT_MATH, setup)
+        assert got[f:f + n].tobytes() == want.tobytes(), "scene %d" % k
+
+
+@pytest.mark.gpu
+def test_batch_with_warm_start_equals_scenes_alone(cuda_lib):
+    """The learned warm start on a batch: every quantity the network sees is per particle, so each
+    scene comes out as if stepped alone with the same network."""
+    from akuaengine_gb300.warm_start import LambdaNet
+
+    net = LambdaNet(seed=3)
+    net.set_normalization(np.zeros(8, np.float32), np.ones(8, np.float32), 1e-6, blend=0.5)
+    b = scene.batched_dam_breaks(count=3, n_min=800, n_max=5000, seed=12)
+    cfg, corr = scene.benchmark_params()
+    cfg = dataclasses.replace(cfg, solverIterations=2)
+
+    def setup(s):
+        s.set_lambda_tracking(True)
+        s.set_warm_start(net)
+
+    steps = 4
+    got = _batch_with(b, cfg, corr, steps, 0, setup)
+    for k, d in enumerate(b.scenes):
+        f, n = b.first[k], d["numParticles"]
+        want = _alone_with(b, k, cfg, corr, steps, 0, setup)
+        assert got[f:f + n].tobytes() == want.tobytes(), "scene %d" % k
+    net.close()
