@@ -18,8 +18,11 @@ step in colour[3], `tag`).  The local step must use the whole scene's hash table
 (maxNeighbours * N), so hashes and bucket collisions are those of the single-domain step.
 
 The local step is any callable that steps an array of records in place (the GPU solver on a box
-with one GPU per rank; the host restatement in the tests).  This implementation gives every rank
-the whole scene's records at the start of a step and gathers the owned results after it.
+with one GPU per rank; the host restatement in the tests).  Every rank gets the whole scene's
+records at the start of a step and the owned results are gathered after it.  Two forms: numpy
+record arrays (`decomposed_step`) and device-resident torch tensors of the attached-buffer layout
+(`decomposed_step_device`, selection and reassembly on the GPU, exchange through
+`all_gather_records`, which uses torch.distributed: NCCL for CUDA tensors).
 """
 from __future__ import annotations
 
@@ -119,3 +122,83 @@ def decomposed_step(records: np.ndarray, world: int, cfg, dt: float, local_step,
     out = global_records(mine, records.shape[0])
     out["color"][:, 3] = records["color"][:, 3][out["color"][:, 3].astype(np.int64)]
     return out
+
+
+# ------------------------------------------------------------------------------ device-resident
+# The same decomposition on records that stay on the GPU: a torch uint8 tensor of N x 108-byte
+# records (the attached-buffer layout).  Selection, tagging and reassembly are torch operations on
+# the device; the local step is any callable stepping a record tensor in place (the CUDA solver).
+REC_BYTES = 108
+REC_WORDS = REC_BYTES // 4
+_W_X, _W_V, _W_HASH, _W_TAG = 0, 3, 21, 25  # word offsets: position.x, velocity, hash, colour[3]
+
+
+def _rows(buf):
+    n = buf.numel() // REC_BYTES
+    return buf.view(n, REC_BYTES), n
+
+
+def decomposed_step_device(records, world: int, cfg, dt: float, local_step, exchange=None,
+                           rank: int | None = None, margin: float = 0.0):
+    """One decomposed step of device-resident records (`records`: contiguous torch uint8 tensor of
+    N x 108 bytes on a GPU).  Without `exchange` every rank's slab is stepped here in turn; with it
+    (a callable taking this rank's owned records and returning every rank's, e.g.
+    `all_gather_records`), this process steps rank `rank` only.  Returns a new tensor with the whole
+    scene's records in global hash order, equal to the single-domain step's."""
+    import torch
+
+    rows, n = _rows(records)
+    if n >= (1 << 24):
+        raise ValueError("too many particles to tag in a float32")
+    tagged = rows.clone()
+    tw = tagged.view(torch.float32)                       # [N, 27]
+    tw[:, _W_TAG] = torch.arange(n, device=records.device, dtype=torch.float32)
+    x = tw[:, _W_X].double()
+    x_min = x.min()
+    x_max = torch.nextafter(x.max(), torch.tensor(float("inf"), dtype=torch.float64,
+                                                  device=records.device))
+    v_max = float(tw[:, _W_V:_W_V + 3].double().norm(dim=1).max())
+    g = float(np.linalg.norm(np.asarray(cfg.gravity, dtype=np.float64)))
+    halo = halo_width(cfg.smoothRadius, cfg.solverIterations, v_max, dt, g, margin)
+    width = (x_max - x_min) / world
+    owner = torch.clamp(torch.floor((x - x_min) / width).long(), 0, world - 1)
+    ranks = range(world) if exchange is None else [rank]
+    mine = []
+    for r in ranks:
+        lo = -float("inf") if r == 0 else float(x_min + r * width) - halo
+        hi = float("inf") if r == world - 1 else float(x_min + (r + 1) * width) + halo
+        idx = torch.nonzero(((x >= lo) & (x < hi)) | (owner == r)).squeeze(1)  # global order kept
+        local = tagged[idx].contiguous()
+        local_step(local.view(-1))
+        tags = local.view(torch.float32)[:, _W_TAG].long()
+        mine.append(local[owner[tags] == r])
+    if exchange is not None:
+        mine = exchange(mine[0])
+    allrec = torch.cat(mine)
+    if allrec.shape[0] != n:
+        raise RuntimeError("every particle must have exactly one owner")
+    hashes = allrec.view(torch.int32)[:, _W_HASH].long() & 0xFFFFFFFF
+    prev = allrec.view(torch.float32)[:, _W_TAG].long()
+    out = allrec[torch.argsort(hashes * n + prev)]       # (hash, previous global rank): unique
+    ow = out.view(torch.float32)
+    ow[:, _W_TAG] = rows.view(torch.float32)[ow[:, _W_TAG].long(), _W_TAG]
+    return out.view(-1)
+
+
+def all_gather_records(mine, group=None):
+    """Every rank's owned records (torch uint8 [k, 108], k differing between ranks) through
+    torch.distributed.all_gather (NCCL for CUDA tensors, gloo for CPU ones): sizes first, then
+    contributions padded to the largest."""
+    import torch
+    import torch.distributed as dist
+
+    world = dist.get_world_size(group)
+    size = torch.tensor([mine.shape[0]], device=mine.device, dtype=torch.int64)
+    sizes = [torch.zeros_like(size) for _ in range(world)]
+    dist.all_gather(sizes, size, group=group)
+    sizes = [int(s.item()) for s in sizes]
+    padded = torch.zeros((max(sizes), REC_BYTES), dtype=torch.uint8, device=mine.device)
+    padded[:mine.shape[0]] = mine
+    parts = [torch.empty_like(padded) for _ in range(world)]
+    dist.all_gather(parts, padded, group=group)
+    return [p[:k] for p, k in zip(parts, sizes)]
