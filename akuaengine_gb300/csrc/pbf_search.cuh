@@ -45,6 +45,7 @@ constexpr size_t kSearchSmem =
     sizeof(uint32_t) * kSearchBlock * kListRow + sizeof(float4) * kSearchBlock;
 constexpr uint32_t kFullWarp = 0xffffffffu;
 constexpr uint32_t kMixedBucket = 0x80000000u;  // bucket table: y bit for a mixed bucket
+constexpr uint32_t kDenseRun = 2048;  // candidates of a run beyond which the walk may stop early
 
 template <bool EXACT>
 __global__ void __launch_bounds__(kSearchBlock)
@@ -111,7 +112,8 @@ __global__ void __launch_bounds__(kSearchBlock)
         const uint32_t off = incl - blen;  // lanes 27..31: the sequence length
         const uint32_t total = __shfl_sync(kFullWarp, incl, 31);
 
-        for (uint32_t c0 = 0; c0 < total; c0 += 32) {
+        // one chunk of 32 candidates of the run's sequence
+        auto chunk = [&](uint32_t c0) {
             const uint32_t at = c0 + lane;
             int b = 0;  // the last bucket starting at or before `at`
 #pragma unroll
@@ -164,6 +166,20 @@ __global__ void __launch_bounds__(kSearchBlock)
                 const int pos = __shfl_sync(kFullWarp, count, q) + __popc(bal & below);
                 if (hit) place(q, pos);
                 if (lane == q) count += __popc(bal);
+            }
+        };
+        if (total <= kDenseRun) {
+            for (uint32_t c0 = 0; c0 < total; c0 += 32) chunk(c0);
+        } else {
+            // a pile-up far denser than any cell of a resting fluid: stop once every list of the
+            // run is full (later hits are neither stored nor needed for the overflow flag; a list
+            // fills only after at least cap candidates), or such a run would cost run size x
+            // sequence length tests
+            for (uint32_t c0 = 0; c0 < total; c0 += 32) {
+                if (c0 >= (uint32_t)cap &&
+                    __all_sync(kFullWarp, lane < q0 || lane >= q1 || count >= cap))
+                    break;
+                chunk(c0);
             }
         }
     }

@@ -124,6 +124,28 @@ def test_capacity_truncation_bitexact():
     assert_records_bitexact(g, o)
 
 
+def test_dense_pile_up_bitexact():
+    """5,000 particles packed into one cell beside a resting block: their run's candidate sequence
+    is far longer than any resting cell's, so the walk stops once every list of the run is full;
+    lists, records and the overflow flag must still equal the oracle's, which walks everything."""
+    sc = scene.dam_break((12, 12, 12), (3.0, 3.0, 3.0), seed=4)
+    rng = np.random.default_rng(4)
+    pile = np.zeros(5000, dtype=sc.particles.dtype)
+    pile["position"] = (np.array([0.95, 0.55, 0.95]) + rng.uniform(0.0, 0.09, (5000, 3))).astype(
+        np.float32)
+    pile["mass"] = 1.0
+    pile["color"] = (1.0, 0.0, 0.0, 1.0)
+    pile["size"] = 50.0
+    sc.particles = np.concatenate([sc.particles, pile])
+    cfg, corr = PBFConfig(), LambdaCorrParams()
+    g, ge = run_gpu(sc, cfg, corr, 2, ak.OPT_EXACT_MATH)
+    o, oe = run_oracle(sc, cfg, corr, 2)
+    assert ge["cnt"].max() == cfg.maxNeighbours
+    assert ge["stats"]["deviceFlags"] & ak.FLAG_CAP_REACHED
+    assert_grid_equal(ge, oe, cfg.maxNeighbours)
+    assert_records_bitexact(g, o)
+
+
 @pytest.mark.parametrize("cap", [128, 100, 200])
 @pytest.mark.parametrize("table_size", [None, 4096])
 def test_long_lists_bitexact(cap, table_size):
