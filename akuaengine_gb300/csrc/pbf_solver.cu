@@ -347,15 +347,15 @@ void enqueue_pairs(akua_pbf* s, cudaStream_t st, Marker& mark) {
             akua::k_delta_final<EXACT><<<gp(2), pb[2], 0, st>>>(
                 s->d_params, cur, s->lam, nbr4, s->cnt, s->x4g, s->x4, s->v4, s->vstar4, s->dp4,
                 s->col4g, s->sizeg, s->col4, s->size, s->rrefg, s->rref, s->rhog, s->lamg, s->dpg,
-                s->rho, s->lam, 1, s->psl, s->mass_bits, s->xv8);
+                s->rho, nullptr, 1, s->psl, s->mass_bits, s->xv8);  // lam_out: zero iterations only
             mark("k_delta_final");
         }
     }
     if (iters == 0) {
         akua::k_delta_final<EXACT><<<gp(2), pb[2], 0, st>>>(
-            s->d_params, s->ps0, s->lam, nbr4, s->cnt, s->x4g, s->x4, s->v4, s->vstar4, s->dp4,
+            s->d_params, s->ps0, nullptr, nbr4, s->cnt, s->x4g, s->x4, s->v4, s->vstar4, s->dp4,
             s->col4g, s->sizeg, s->col4, s->size, s->rrefg, s->rref, s->rhog, s->lamg, s->dpg,
-            s->rho, s->lam, 0, s->psl, s->mass_bits, s->xv8);
+            s->rho, s->lam, 0, s->psl, s->mass_bits, s->xv8);  // no delta: lambda is not read
         mark("k_delta_final");
     }
     // psl is free after the last delta: it carries (x, |omega|) to confinement
