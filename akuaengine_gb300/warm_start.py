@@ -18,7 +18,6 @@ import ctypes
 
 import numpy as np
 
-from . import _abi
 from ._abi import MLP_NORM, MLP_PARAMS, check, load_library
 
 PARAM_SHAPES = [("W1", (64, 8)), ("b1", (64,)), ("W2", (64, 64)), ("b2", (64,)),
