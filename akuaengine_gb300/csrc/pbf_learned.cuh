@@ -1,5 +1,5 @@
 // Learned warm start of the Jacobi loop: per-particle features for the lambda network, and the
-// density-constraint error that judges a step (plain or warm-started).
+// density-constraint error that measures a step (plain or warm-started).
 //
 // The warm start replaces iteration 1's lambda (the one-step Jacobi estimate) by the network's
 // prediction of the lambda a 20-iteration solve accumulates over the step (the sum of its

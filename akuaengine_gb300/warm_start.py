@@ -4,7 +4,7 @@ The network (C ABI `akua_mlp_*`, tensor-core kernels in csrc/mlp.cuh) predicts, 
 features of a particle at the start of a step, the lambda that a long plain solve accumulates
 over that step.  A solver with the network attached (`PBFSolver.set_warm_start`) uses the
 prediction in its first Jacobi iteration and runs its remaining iterations unchanged; the plain
-iterated solver stays the fallback (detach the network) and `PBFSolver.density_error` judges both.
+iterated solver stays the fallback (detach the network) and `PBFSolver.density_error` measures both.
 
 Training pairs come from the solver itself: a "teacher" solver runs the scene with many
 iterations (20 by default) and `capture_training` records, every few steps, the features at the

@@ -23,6 +23,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -125,7 +126,7 @@ class ClockSampler:
 
     def start(self):
         try:
-            self.out = open(os.devnull if False else self._path(), "w")
+            self.out = open(self._path(), "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
                  "-lms", "200", "-i", str(self.device)], stdout=self.out, stderr=subprocess.DEVNULL)
@@ -133,8 +134,8 @@ class ClockSampler:
             self.proc = None
 
     def _path(self):
-        d = os.path.join(ROOT, "gpurun_out") if os.path.isdir(os.path.join(ROOT, "gpurun_out")) \
-            else "/tmp"
+        # the raw samples: AKUA_BENCH_CLOCKS_DIR when set, else the temporary directory
+        d = os.environ.get("AKUA_BENCH_CLOCKS_DIR") or tempfile.gettempdir()
         return os.path.join(d, "bench_clocks_%d_%d.csv" % (self.device, os.getpid()))
 
     def stop(self):
