@@ -1,11 +1,12 @@
 // Host side of the GB300 PBF step: device memory, the per-step launch sequence, CUDA-graph
 // capture and the C ABI declared in include/akua_pbf.h.
 //
-// One handle = one particle set on one device.  A step is [params] [import] and then the captured
-// body: keys -> radix sort by (hash, previous reference rank) -> radix sort by Morton cell ->
-// gather into the new internal order -> reference-order tables -> neighbour walk (+ iteration 1
-// density/lambda) -> (delta+correct, density+lambda) x iterations -> delta+update+damping ->
-// vorticity -> confinement -> XSPH -> export in reference order.  Nothing on this path copies to
+// One handle = one particle set on one device.  A step is [params] [import + sort keys, or the
+// keys alone when the state stayed on the device] and then the captured body: radix sort by
+// (hash, previous reference rank) beside radix sort by Morton cell -> gather into the new internal
+// order -> bucket table -> neighbour walk (+ iteration 1 density/lambda) -> (delta+correct,
+// density+lambda) x iterations -> delta+update+damping -> vorticity -> confinement -> XSPH (which
+// also empties the bucket table) -> export in reference order.  Nothing on this path copies to
 // the host or synchronises; the reference instead synchronises after every kernel and moves the
 // neighbour lists through host memory four times per step (PBFSolver.h:23-24,
 // NeighbourSearchCUDA.cu:151-154, 182-183, ConstraintSolverCUDA.cu:195-198,
