@@ -15,8 +15,8 @@
 // in the reference's walk order.
 //
 // Reference stages (paths relative to the AkuaEngine tree) and the kernels that cover them:
-//   predict              IntegrationCUDA.cu:27-36            k_keys, k_gather
-//   cell hash            NeighbourSearchCUDA.cu:15-44        k_keys
+//   predict              IntegrationCUDA.cu:27-36            k_import or k_keys, k_gather
+//   cell hash            NeighbourSearchCUDA.cu:15-44        k_import or k_keys (write_keys)
 //   sort by hash         NeighbourSearchCUDA.cu:167-170      radix sort of (hash, previous rank)
 //   bucket starts        NeighbourSearchCUDA.cu:52-65        k_table_build
 //   neighbour walk       NeighbourSearchCUDA.cu:72-130       k_search (+ iteration 1 density/lambda)
