@@ -61,10 +61,11 @@ inline int bits_for(uint64_t bound) {  // keys are < bound
     return bits < 1 ? 1 : bits;
 }
 
-// counts[d * tiles + tile] = keys of `tile` with digit d; totals[d] += the same.
+// counts[d * tiles + tile] = keys of `tile` with digit d; totals[d] += the same.  A key's digit
+// is (key >> shift) & digit_mask; digit_mask < RADIX narrows a pass to fewer bits than BITS.
 template <int BITS>
 __global__ void __launch_bounds__(BLOCK) upsweep(const uint32_t* __restrict__ keys, int n, int shift,
-                                                 uint32_t* __restrict__ counts,
+                                                 uint32_t digit_mask, uint32_t* __restrict__ counts,
                                                  uint32_t* __restrict__ totals, int tiles) {
     constexpr int RADIX = 1 << BITS;
     __shared__ uint32_t hist[WARPS][RADIX];
@@ -75,7 +76,7 @@ __global__ void __launch_bounds__(BLOCK) upsweep(const uint32_t* __restrict__ ke
 #pragma unroll 4
     for (int r = 0; r < ROUNDS; ++r) {
         const int idx = base + r * 32;
-        if (idx < n) atomicAdd(&hist[warp][(keys[idx] >> shift) & (RADIX - 1)], 1u);
+        if (idx < n) atomicAdd(&hist[warp][(keys[idx] >> shift) & digit_mask], 1u);
     }
     __syncthreads();
     for (int d = threadIdx.x; d < RADIX; d += BLOCK) {
@@ -136,7 +137,8 @@ template <int BITS>
 __global__ void __launch_bounds__(BLOCK)
     downsweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
               uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, int n, int shift,
-              const uint32_t* __restrict__ offsets, int tiles, uint32_t* __restrict__ rank_out) {
+              uint32_t digit_mask, const uint32_t* __restrict__ offsets, int tiles,
+              uint32_t* __restrict__ rank_out) {
     constexpr int RADIX = 1 << BITS;
     extern __shared__ uint32_t wbase_flat[];  // [WARPS][RADIX]
     uint32_t(*wbase)[RADIX] = reinterpret_cast<uint32_t(*)[RADIX]>(wbase_flat);
@@ -158,7 +160,7 @@ __global__ void __launch_bounds__(BLOCK)
     for (int r = 0; r < ROUNDS; ++r) {
         const int idx = base + r * 32;
         const bool valid = idx < n;
-        const uint32_t d = valid ? ((key[r] >> shift) & (RADIX - 1)) : 0xffffffffu;
+        const uint32_t d = valid ? ((key[r] >> shift) & digit_mask) : 0xffffffffu;
         const uint32_t peers = __match_any_sync(0xffffffffu, d);
         uint32_t before = 0;
         if (valid) before = wbase[warp][d];
@@ -182,7 +184,7 @@ __global__ void __launch_bounds__(BLOCK)
     for (int r = 0; r < ROUNDS; ++r) {
         const int idx = base + r * 32;
         if (idx < n) {
-            const uint32_t d = (key[r] >> shift) & (RADIX - 1);
+            const uint32_t d = (key[r] >> shift) & digit_mask;
             const uint32_t dst = wbase[warp][d] + rank[r];
             keys_out[dst] = key[r];
             vals_out[dst] = val[r];
@@ -191,18 +193,20 @@ __global__ void __launch_bounds__(BLOCK)
     }
 }
 
+// One pass over the digit (key >> shift) & digit_mask; digit_mask defaults to all BITS bits.
 template <int BITS, class Mark>
 inline void run_pass(cudaStream_t s, const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
                      uint32_t* vout, uint32_t* counts, uint32_t* totals, int n, int shift,
-                     uint32_t* rank_out, Mark& mark) {
+                     uint32_t* rank_out, Mark& mark, uint32_t digit_mask = (1u << BITS) - 1u) {
     const int tiles = num_tiles(n);
     constexpr int RADIX = 1 << BITS;
-    upsweep<BITS><<<tiles, BLOCK, 0, s>>>(kin, n, shift, counts, totals, tiles);
+    digit_mask &= RADIX - 1;  // the kernels' shared-memory tables hold RADIX digits
+    upsweep<BITS><<<tiles, BLOCK, 0, s>>>(kin, n, shift, digit_mask, counts, totals, tiles);
     mark("radix_upsweep");
     scan_rows<<<RADIX, SCAN_BLOCK, 0, s>>>(counts, totals, tiles);
     mark("radix_scan");
     downsweep<BITS><<<tiles, BLOCK, WARPS * RADIX * sizeof(uint32_t), s>>>(
-        kin, vin, kout, vout, n, shift, counts, tiles, rank_out);
+        kin, vin, kout, vout, n, shift, digit_mask, counts, tiles, rank_out);
     mark("radix_downsweep");
 }
 

@@ -1,12 +1,11 @@
 // akua_sort_pairs_noalloc: the step's stable radix sort of (key, value) pairs for callers that
-// must not allocate device memory.
+// cannot allocate device memory.
 //
-// Some callers cannot call cudaMalloc: code that records its work into a CUDA graph under stream
-// capture (allocation calls are not capturable), host applications whose device memory is owned
-// by their own allocator or a fixed budget, and real-time frame loops where an allocation's
-// implicit synchronisation would stall the frame.  This entry point therefore keeps all of its
-// temporary storage in one file-scope device array of fixed size; the caller passes only inputs
-// and outputs.
+// Some callers of this library cannot call cudaMalloc: host applications whose device memory is
+// owned by their own allocator or held to a fixed budget (a game engine's or renderer's heap), and
+// real-time frame loops where an allocation's implicit device synchronisation would stall the
+// frame.  This entry point therefore keeps all of its temporary storage in one file-scope device
+// array of fixed size; the caller passes only inputs and outputs.
 //
 // The array is shared by every call in the process, keeps the last call's contents, and is
 // resident on every device that loads the library until the process exits.  Calls whose work
@@ -37,6 +36,13 @@ struct NoMark {
     void operator()(const char*) {}
 };
 
+// True when the byte ranges [a, a + bytes) and [b, b + bytes) share a byte.
+bool overlap(const void* a, const void* b, size_t bytes) {
+    if (!a || !b) return false;
+    const uintptr_t x = reinterpret_cast<uintptr_t>(a), y = reinterpret_cast<uintptr_t>(b);
+    return x < y + bytes && y < x + bytes;
+}
+
 }  // namespace
 
 static __device__ __align__(256) uint32_t g_sort_scratch[kScratchWords];
@@ -47,8 +53,10 @@ constexpr int kMaxDevices = 64;
 std::mutex g_mutex;
 uint32_t* g_scratch[kMaxDevices] = {};
 
-// Device address of g_sort_scratch on the current device, looked up on the first call per device.
-// In host code the array's name is only a host-side stand-in; the kernels need this address.
+// Device address of g_sort_scratch on the current device, looked up on the first call per device
+// and kept for the life of the process (a cudaDeviceReset between calls is not supported: it
+// unloads the module that holds the array).  In host code the array's name is only a host-side
+// stand-in; the kernels need this address.
 cudaError_t scratch_address(uint32_t** out) {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
@@ -74,7 +82,12 @@ extern "C" int akua_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* 
     if (n > kMaxPairs) return AKUA_ERR_TOO_LARGE;
     if (n == 0) return AKUA_OK;
     if (!keys_in || !keys_out || !vals_out) return AKUA_ERR_INVALID_ARGUMENT;
-    if (keys_in == keys_out || vals_out == keys_out || (vals_in && vals_in == vals_out))
+    // the passes read the inputs while other blocks write the outputs: no two of the four arrays
+    // may share memory, except the two inputs (both are only read)
+    const size_t bytes = sizeof(uint32_t) * (size_t)n;
+    if (overlap(keys_out, vals_out, bytes) || overlap(keys_in, keys_out, bytes) ||
+        overlap(keys_in, vals_out, bytes) || overlap(vals_in, keys_out, bytes) ||
+        overlap(vals_in, vals_out, bytes))
         return AKUA_ERR_INVALID_ARGUMENT;
     uint32_t* scratch = nullptr;
     cudaError_t e = scratch_address(&scratch);
@@ -98,15 +111,18 @@ extern "C" int akua_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* 
         uint32_t* kout = to_out ? keys_out : tmp_keys;
         uint32_t* vout = to_out ? vals_out : tmp_vals;
         uint32_t* tot = totals + (size_t)p * akua::radix::MAX_RADIX;
+        // the digit covers only this pass's bits, so key bits at and above key_bits never
+        // influence the order (a pass narrower than 8 bits still runs the 8-bit kernels)
+        const uint32_t mask = (1u << plan.width[p]) - 1u;
         if (plan.width[p] <= 8)
             akua::radix::run_pass<8>(st, kin, vin, kout, vout, counts, tot, n, plan.shift[p],
-                                      nullptr, mark);
+                                      nullptr, mark, mask);
         else if (plan.width[p] == 9)
             akua::radix::run_pass<9>(st, kin, vin, kout, vout, counts, tot, n, plan.shift[p],
-                                      nullptr, mark);
+                                      nullptr, mark, mask);
         else
             akua::radix::run_pass<10>(st, kin, vin, kout, vout, counts, tot, n, plan.shift[p],
-                                      nullptr, mark);
+                                      nullptr, mark, mask);
         kin = kout;
         vin = vout;
     }

@@ -174,17 +174,20 @@ int akua_pbf_profile_begin(akua_pbf* solver, int32_t maxSteps);
 int akua_pbf_profile_end(akua_pbf* solver, akua_kernel_time* out, int32_t capacity, int32_t* count);
 
 /* No counterpart in the reference.  The step's stable radix sort of (key, value) pairs, for
- * callers that cannot allocate device memory: code recording into a CUDA graph under stream
- * capture (allocation is not capturable), applications whose device memory belongs to their own
- * allocator or budget, and frame loops that cannot afford an allocation's synchronisation.
- * Sorts the n pairs (keysIn[i], valsIn[i]) by the low keyBits bits of the key, ties in input
- * order, into keysOut / valsOut (device arrays; inputs are not modified and must not overlap the
- * outputs).  valsIn == NULL makes each key's index its payload.  Asynchronous on cudaStream.
+ * callers that cannot allocate device memory: applications whose device memory belongs to their
+ * own allocator or a fixed budget, and frame loops that cannot afford an allocation's implicit
+ * device synchronisation.
+ * Sorts the n pairs (keysIn[i], valsIn[i]) by the low keyBits bits of the key (higher key bits
+ * are ignored), ties in input order, into keysOut / valsOut (device arrays; keysOut receives the
+ * whole keys).  The inputs are not modified; no output may overlap an input or the other output
+ * (AKUA_ERR_INVALID_ARGUMENT).  valsIn == NULL makes each key's index its payload.  Asynchronous
+ * on cudaStream.
  * Temporary storage is one fixed device array inside the library (about 9.5 MB, held on every
  * device that loads the library until exit); nothing is allocated, and n above
  * AKUA_SORT_NOALLOC_MAX_PAIRS returns AKUA_ERR_TOO_LARGE.  The first call on a device looks up
- * that array's device address, so make it before any stream capture.  Every call shares the
- * array: calls that overlap on the GPU race and must be ordered by the caller. */
+ * that array's device address and keeps it, so make that call before any stream capture, and do
+ * not call cudaDeviceReset between calls.  Every call shares the array: calls that overlap on the
+ * GPU race and must be ordered by the caller. */
 #define AKUA_SORT_NOALLOC_MAX_PAIRS (1 << 20)
 int akua_sort_pairs_noalloc(const uint32_t* keysIn, const uint32_t* valsIn, uint32_t* keysOut,
                             uint32_t* valsOut, int32_t n, int32_t keyBits, void* cudaStream);

@@ -17,7 +17,6 @@ import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
-DEFAULT_REF = "/root/reference"
 UNITS = ["NeighbourSearchCUDA", "ConstraintSolverCUDA", "IntegrationCUDA"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -34,8 +33,12 @@ def have_cubins() -> bool:
     return all(os.path.exists(p) for p in cubin_paths())
 
 
-def build_cubins(ref_root: str = DEFAULT_REF) -> list[str]:
-    """Reference flags (CMakeLists.txt:66-70: --extended-lambda -diag-suppress=20012), sm_103a."""
+def build_cubins(ref_root: str | None = None) -> list[str]:
+    """Reference flags (CMakeLists.txt:66-70: --extended-lambda -diag-suppress=20012), sm_103a.
+    `ref_root` defaults to oracle/ref_root.py's lookup."""
+    from oracle.ref_root import require_reference_root
+
+    ref_root = require_reference_root(ref_root)
     os.makedirs(REF_DIR, exist_ok=True)
     out = []
     for u in UNITS:
