@@ -157,6 +157,8 @@ def batched_dam_breaks(count=256, n_min=2000, n_max=64000, h=0.1, seed=0, dt=0.0
 def workload(name: str, seed: int = 0) -> Scene:
     if name == "dam_break_27k":
         return dam_break((30, 30, 30), (4.0, 4.0, 4.0), seed=seed)
+    if name == "dam_break_100k":
+        return dam_break((50, 40, 50), (3.0, 1.5, 1.5), seed=seed)
     if name == "dam_break_1m":
         return dam_break((100, 100, 100), (3.0, 1.5, 1.5), seed=seed)
     if name == "double_dam_break_8m":

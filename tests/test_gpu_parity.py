@@ -501,17 +501,21 @@ def _ref_cases():
 @pytest.mark.parametrize("name", list(_ref_cases()))
 def test_cuda_matches_reference_kernels(name, opts):
     from make_ref_gpu_golden import tagged
-    from test_reference_golden import compare_floats, load
+    from test_reference_golden import (assert_order_equal, compare_floats, fp32_sensitivity,
+                                       golden_floats, have_fixture, load)
 
     make, cfg, corr, steps, lists = _ref_cases()[name]
+    if not have_fixture(name):
+        pytest.skip("fixture not generated")
     ref = load(name)
     sc = make()
     g, ge = run_gpu(sc, cfg, corr, steps, opts, particles=tagged(sc))
     assert np.array_equal(g["hash"], ref["hash"])
-    assert np.array_equal(g["color"], ref["color"]), "sorted order differs"
+    assert_order_equal(g, ref)
     if lists:
         assert np.array_equal(ge["cnt"], ref["cnt"])
         flat = np.concatenate([ge["nbr"][i, : ge["cnt"][i]] for i in range(sc.n)])
         assert np.array_equal(flat, ref["nbr_flat"])
     # the fast path adds its own rsqrt-level error on top of the oracle's
-    compare_floats(g, ref, scale=1.0 if opts else 3.0)
+    compare_floats(golden_floats(g, name), ref, scale=1.0 if opts else 3.0,
+                   extra=fp32_sensitivity(name))
