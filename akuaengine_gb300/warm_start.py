@@ -23,8 +23,8 @@ from ._abi import MLP_NORM, MLP_PARAMS, check, load_library
 PARAM_SHAPES = [("W1", (64, 8)), ("b1", (64,)), ("W2", (64, 64)), ("b2", (64,)),
                 ("W3", (64, 64)), ("b3", (64,)), ("w4", (64,)), ("b4", (1,))]
 FEATURE_NAMES = ["density_constraint", "neighbours_over_32", "lambda_denominator",
-                 "lambda_iteration_1", "previous_lambda_sum", "mean_neighbour_constraint",
-                 "velocity_divergence", "speed"]
+                 "lambda_iteration_1", "previous_lambda_sum", "grad_constraint_norm",
+                 "grad_constraint_along_gravity", "speed"]
 
 
 def init_params(seed: int = 0) -> np.ndarray:
@@ -273,3 +273,79 @@ def calibrate_blend(net: LambdaNet, sc, cfg, corr, iterations: int,
         best = min((g for g in res if res[g][0] <= bound), key=lambda g: (res[g][1], res[g][0]))
     net.set_blend(best)
     return res
+
+
+def calibrate_equal_error(net: LambdaNet, sc, cfg, corr, iterations: int, target_max: float,
+                          blends=(0.25, 0.5, 0.75, 1.0), steps: int = 60, stream=None):
+    """Zero-tolerance calibration against a plain solver's max error: rolls `sc` out with each
+    blend at `iterations` warm-started iterations and keeps the blends whose max density error
+    (mean over the rollout of the per-step max) is at most `target_max`.  Sets and returns the
+    one of them with the lowest mean |C|, or None (blend left at 0) when none qualifies; also
+    returns {blend: (max C, mean |C|)}."""
+    res = {}
+    for g in blends:
+        net.set_blend(float(g))
+        e = rollout_errors(sc, cfg, corr, iterations, net, steps, stream)
+        res[float(g)] = ((float(e[:, 0].mean()), float(e[:, 1].mean()))
+                         if np.isfinite(e).all() else (float("inf"), float("inf")))
+    ok = [g for g in res if res[g][0] <= target_max]
+    best = min(ok, key=lambda g: (res[g][1], res[g][0])) if ok else None
+    net.set_blend(best if best is not None else 0.0)
+    return best, res
+
+
+def collect_mixed(scenes, corr, teacher_iterations: int, stream=None, collect=None):
+    """Training pairs from several scenes: `scenes` is a list of (scene, config) (each config
+    carries its scene's gravity); pairs of all scenes concatenated."""
+    import torch
+
+    collect = collect or {"steps": 90, "capture_every": 3, "first_capture": 2}
+    xs, ys = [], []
+    for sc, cfg in scenes:
+        x, y = collect_pairs(sc, cfg, corr, teacher_iterations=teacher_iterations, stream=stream,
+                             **collect)
+        xs.append(x)
+        ys.append(y)
+    return torch.cat(xs), torch.cat(ys)
+
+
+def fewest_iterations_at_equal_error(train_scenes, corr, *, plain_iterations: int = 4,
+                                     candidates=(1, 2, 3), steps: int = 60, stream=None,
+                                     collect=None, epochs: int = 6, batch: int = 65536,
+                                     blends=(0.25, 0.5, 0.75, 1.0), seed: int = 0,
+                                     keep_last: bool = False):
+    """The learned warm start at equal max error.  `train_scenes`: list of (scene, config); the
+    first is also the calibration scene.  For k = candidates in increasing order, trains a network
+    whose target is the lambda sum of a (plain_iterations - k + 1)-iteration teacher (the learned
+    first iteration stands in for the plain iterations it saves) on pairs from every training
+    scene, calibrates its blend with zero tolerance against the plain solver's max error on the
+    calibration scene, and stops at the first k that reaches it.  Returns (k, net or None, report);
+    k = plain_iterations and no network when no candidate qualifies (with `keep_last`, the last
+    candidate's network, blend set to its lowest-max-error blend, is returned as report["last"]
+    for timing and reporting)."""
+    cal_sc, cal_cfg = train_scenes[0]
+    plain = rollout_errors(cal_sc, cal_cfg, corr, plain_iterations, None, steps, stream)
+    target = float(plain[:, 0].mean())
+    report = {"plain_max": target, "plain_mean_abs": float(plain[:, 1].mean()), "tried": {}}
+    ks = sorted(candidates)
+    for k in ks:
+        teacher = plain_iterations - k + 1
+        x, y = collect_mixed(train_scenes, corr, teacher, stream, collect)
+        net = LambdaNet(seed=seed)
+        net.fit_normalization(x, y)
+        train(net, x, y, epochs=epochs, batch=batch, stream=stream)
+        pairs = int(x.shape[0])
+        del x, y
+        best, res = calibrate_equal_error(net, cal_sc, cal_cfg, corr, k, target, blends, steps,
+                                          stream)
+        report["tried"][str(k)] = {"teacher_iterations": teacher, "blend": best, "pairs": pairs,
+                                   "blends": {str(g): [round(v[0], 5), round(v[1], 5)]
+                                              for g, v in res.items()}}
+        if best is not None:
+            return k, net, report
+        if keep_last and k == ks[-1]:
+            net.set_blend(min(res, key=lambda g: res[g][0]))
+            report["last"] = (k, net)
+        else:
+            net.close()
+    return plain_iterations, None, report

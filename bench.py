@@ -18,6 +18,7 @@ from __future__ import annotations
 
 import argparse
 import csv
+import dataclasses
 import json
 import os
 import statistics
@@ -84,6 +85,17 @@ def parse_args(argv=None):
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--profile-steps", type=int, default=10)
+    ap.add_argument("--preroll", type=int, default=240,
+                    help="untimed steps before warm-up: the timed window then lies in the middle "
+                         "of the workload's 500-step run (developed flow), not at rest")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="skip timing the reference's own kernels (baseline leg)")
+    ap.add_argument("--pair-blocks", default=None,
+                    help="six comma-separated block sizes of the pair kernels instead of the "
+                         "autotuner's choice (profiling runs)")
+    ap.add_argument("--resident", action="store_true",
+                    help="records read only on the first step (the key kernel replaces the import "
+                         "on later steps)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--exact", action="store_true", help="IEEE math in pair terms")
@@ -196,6 +208,70 @@ def time_oracle(sc, cfg, corr, steps, budget_s, threads=0):
     return psps / sc.n, psps, cores, sample
 
 
+def step_error_vs_fp64(solver, sc, cfg, corr):
+    """One fast-math GPU step of the scene's state against the same step of the restatement in
+    FP64 and in FP32 (the checker; outside every timed region): per-particle position error
+    quantiles, so the GPU's error is read against the FP32 arithmetic's own."""
+    import numpy as np
+
+    import oracle
+
+    gpu = sc.particles.copy()
+    solver.step_host(gpu, sc.dt, sc.box_min, sc.box_max)
+    out = {}
+    for name, flags in (("fp32_oracle", oracle.FMA), ("fp64_oracle", oracle.FMA | oracle.FP64)):
+        p = sc.particles.copy()
+        oracle.step(p, oracle.make_params(cfg, corr, sc.dt, sc.box_min, sc.box_max, n=sc.n,
+                                          flags=flags))
+        out[name] = p
+    def q(a, b):
+        d = np.abs(a["position"].astype(np.float64) - b["position"]).max(axis=1)
+        return {"p50": float(np.quantile(d, 0.5)), "p99": float(np.quantile(d, 0.99)),
+                "max": float(d.max())}
+    return {"gpu_fast_vs_fp64": q(gpu, out["fp64_oracle"]),
+            "fp32_oracle_vs_fp64": q(out["fp32_oracle"], out["fp64_oracle"]),
+            "gpu_fast_vs_fp32_oracle": q(gpu, out["fp32_oracle"]),
+            "what": "position error after one step of the timed window's state, per particle "
+                    "max over x, y, z"}
+
+
+def time_reference_gpu(sc, cfg, corr, value, e2e):
+    """The reference's unchanged CUDA kernels (compiled from its sources into cubins, driven by a
+    re-sequenced PBFSolver::step) on this GPU and the same state: the faithful form (host-resident
+    neighbour lists, per-step table allocation, as the reference's wrappers do) and the form with
+    device-resident lists.  A baseline leg; returns None-valued entries with the reason when the
+    cubins are absent."""
+    try:
+        from oracle import ref_gpu
+        sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+        from make_ref_gpu_golden import params
+    except Exception as exc:  # noqa: BLE001
+        return {"unavailable": "reference harness not importable: %s" % exc}
+    if not ref_gpu.have_cubins():
+        return {"unavailable": "the reference's kernels were not compiled (oracle/_ref)"}
+    out = {"unit": UNIT}
+    sampler = ClockSampler(0)
+    sampler.start()
+    try:
+        for mode, steps in (("faithful", 10), ("resident", 20)):
+            p = sc.particles.copy()
+            pr = params(cfg, corr, sc, sc.n)
+            pr["warmup"] = 1
+            info = ref_gpu.run(p, pr, steps, mode=mode)
+            v = 1000.0 / info["ms_per_step"]
+            out[mode] = {"steps_per_s": round(v, 3), "ms_per_step": round(info["ms_per_step"], 3),
+                         "steps": steps, "ours_over_reference": round(value / v, 2)}
+            if e2e:
+                out[mode]["ours_e2e_over_reference"] = round(e2e["value"] / v, 2)
+    except Exception as exc:  # noqa: BLE001
+        out["unavailable"] = "reference harness failed: %s" % str(exc)[:200]
+    out["clocks"] = sampler.stop()
+    out["note"] = ("faithful = the reference's wrappers' traffic (host neighbour arrays copied "
+                   "per wrapper, table allocated and filled per step); resident = the same kernels "
+                   "with lists kept on the device")
+    return out
+
+
 def run_reference(args, sc, cfg, corr):
     world, rank, _ = dist_env()
     if rank != 0:
@@ -213,7 +289,11 @@ def run_reference(args, sc, cfg, corr):
         "config": {"workload": args.workload, "particles": sc.n, "solver_iterations": 4,
                    "dt": sc.dt, "hardware": "host CPU cores", "per_step_budget_s": per_step_budget},
         "cpu_baseline": {"value": sps, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": sample, "particle_steps_per_s": psps},
+                         "sample": sample, "particle_steps_per_s": psps,
+                         "precision": "fp32: the reference's arithmetic and contractions, "
+                                      "restated for the host (OpenMP over particles)",
+                         "state": "the workload's initial state (the GPU arm's pre-roll into the "
+                                  "developed flow would take minutes on the host cores)"},
         "e2e": {"value": sps, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference's step is CUDA-only; its algorithm restated on the CPU is timed",
     }
@@ -221,102 +301,131 @@ def run_reference(args, sc, cfg, corr):
 
 
 # ---------------------------------------------------------------------------------- learned
-def run_learned(args, sc, cfg, corr, stream, plain_value, plain_ms):
-    """Learned warm start against the plain 4-iteration step on the same workload: trains the
-    network on pairs from a teacher run (as many plain iterations as the learned first iteration
-    replaces: 4 - 2 + 1 = 3) of a differently seeded copy of the scene
-    (4 captures of every particle), calibrates its blend on that copy, then times the
-    warm-started step with fewer iterations and measures both solvers' density-constraint error
-    over rollouts of the benchmark scene."""
+def _family(cfg, seed, count):
+    """The `count` largest dam breaks of a batched-family draw (config 3's scene distribution),
+    each with its own gravity."""
+    import numpy as np
+
+    from akuaengine_gb300 import PBFConfig, scene
+
+    batch = scene.batched_dam_breaks(count=256, seed=seed)
+    order = np.argsort([-d["numParticles"] for d in batch.scenes])[:count]
+    return [(batch.scene(int(k)),
+             PBFConfig(**{**cfg.__dict__, "gravity": tuple(batch.scenes[int(k)]["gravity"])}))
+            for k in order]
+
+
+def run_learned(args, sc, cfg, corr, stream, plain_value, plain_ms, sc_timed=None):
+    """Learned warm start against the plain 4-iteration step at equal max density error.  Training
+    pairs come from a differently seeded copy of the workload and from dam breaks of the batched
+    family (other block shapes, boxes and gravities).  For k = 1, 2, 3 warm-started iterations
+    (fewest first) a network is trained on a teacher of 4 - k + 1 plain iterations (the learned
+    first iteration stands in for the iterations it saves) and its blend is calibrated on the
+    workload copy with zero tolerance against the plain solver's max error; the first k that
+    reaches it is the equal-error result.  Reported beside it: the k = 3 network timed and
+    evaluated whether or not it qualified.  Steps are device-timed like the main line, from the
+    same state; errors come from scenes not trained on (the benchmark scene, and a batched-family
+    scene of another draw)."""
     import numpy as np
     import torch
 
     from akuaengine_gb300 import PBFSolver, scene
-    from akuaengine_gb300.warm_start import (LambdaNet, calibrate_blend, collect_pairs,
-                                             rollout_errors, train)
+    from akuaengine_gb300.warm_start import fewest_iterations_at_equal_error, rollout_errors
 
     t0 = time.perf_counter()
-    train_sc = scene.workload(args.workload, seed=1)
-    it = args.learned_iterations
-    # the learned first iteration stands in for the plain iterations it saves: the teacher runs
-    # plain_iterations - warm_iterations + 1 iterations and the target is their lambda sum
-    teacher = cfg.solverIterations - it + 1
-    x, y = collect_pairs(train_sc, cfg, corr, steps=123, capture_every=40, first_capture=2,
-                         teacher_iterations=teacher, stream=stream)
+    train_scenes = [(scene.workload(args.workload, seed=1), cfg)] + _family(cfg, 3, 8)
+    plain_it = cfg.solverIterations
+    steps = 60
+    k, net, report = fewest_iterations_at_equal_error(
+        train_scenes, corr, plain_iterations=plain_it, candidates=(1, 2, 3), steps=steps,
+        stream=stream, collect={"steps": 123, "capture_every": 40, "first_capture": 2},
+        keep_last=True)
+    last = report.pop("last", None)
     torch.cuda.synchronize()
     t1 = time.perf_counter()
-    net = LambdaNet(seed=0)
-    net.fit_normalization(x, y)
-    losses = train(net, x, y, epochs=6, batch=65536, stream=stream)
-    torch.cuda.synchronize()
-    t2 = time.perf_counter()
-    steps = 60
-    cal = calibrate_blend(net, train_sc, cfg, corr, iterations=it, steps=steps, stream=stream,
-                          blends=(0.0, 0.25, 0.5, 0.75, 1.0), max_tolerance=0.05)
-    t3 = time.perf_counter()
-    del x, y
+    timed = sc_timed if sc_timed is not None else sc
 
-    # timing: the warm-started step, device-timed like the main line
-    solver = PBFSolver(sc.n, cfg, corr, stream=stream)
-    solver.set_solver_iterations(it)
-    solver.set_warm_start(net)
-    buf = torch.from_numpy(sc.particles.view(np.uint8).copy()).cuda()
-    with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
+    def time_solver(iterations, network):
+        solver = PBFSolver(sc.n, cfg, corr, stream=stream)
+        solver.set_solver_iterations(iterations)
+        if network is not None:
+            solver.set_warm_start(network)
+        buf = torch.from_numpy(timed.particles.view(np.uint8).copy()).cuda()
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup):
+                solver.step(buf, sc.dt, sc.box_min, sc.box_max)
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
             solver.step(buf, sc.dt, sc.box_min, sc.box_max)
-    torch.cuda.synchronize()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    for _ in range(args.steps):
-        solver.step(buf, sc.dt, sc.box_min, sc.box_max)
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    ms = ev0.elapsed_time(ev1)
-    launches = solver.kernels_per_step()
-    solver.profile_begin(3)
-    for _ in range(3):
-        solver.step(buf, sc.dt, sc.box_min, sc.box_max)
-    prof = solver.profile_end()
-    solver.close()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        launches = solver.kernels_per_step()
+        solver.profile_begin(3)
+        for _ in range(3):
+            solver.step(buf, sc.dt, sc.box_min, sc.box_max)
+        prof = solver.profile_end()
+        solver.close()
+        return args.steps / (ms / 1000.0), ms / args.steps, launches, prof
 
-    # accuracy: rollouts from the benchmark scene's initial state
-    e_plain = rollout_errors(sc, cfg, corr, cfg.solverIterations, None, steps, stream)
-    e_warm = rollout_errors(sc, cfg, corr, it, net, steps, stream)
-    e_plain_same = rollout_errors(sc, cfg, corr, it, None, steps, stream)
-    net.close()
-    value = args.steps / (ms / 1000.0)
-    return {
+    evals = {"benchmark_scene_seed0": (sc, cfg), "batched_family_scene": _family(cfg, 7, 1)[0]}
+
+    def accuracy(iterations, network):
+        out = {}
+        for name, (esc, ecfg) in evals.items():
+            e_plain = rollout_errors(esc, ecfg, corr, plain_it, None, steps, stream)
+            e_warm = rollout_errors(esc, ecfg, corr, iterations, network, steps, stream)
+            e_same = rollout_errors(esc, ecfg, corr, iterations, None, steps, stream)
+            out[name] = {
+                "particles": int(esc.n),
+                "warm": {"max": round(float(e_warm[:, 0].mean()), 5),
+                         "mean_abs": round(float(e_warm[:, 1].mean()), 5)},
+                "plain": {"max": round(float(e_plain[:, 0].mean()), 5),
+                          "mean_abs": round(float(e_plain[:, 1].mean()), 5)},
+                "plain_same_iterations": {"max": round(float(e_same[:, 0].mean()), 5),
+                                          "mean_abs": round(float(e_same[:, 1].mean()), 5)},
+                "warm_max_within_plain": bool(e_warm[:, 0].mean() <= e_plain[:, 0].mean())}
+        return out
+
+    value, ms, launches, prof = time_solver(k, net)
+    result = {
         "method": "iteration 1 uses lambda0 + blend * (network estimate - lambda0), then plain "
-                  "Jacobi iterations; blend calibrated on the training scene: lowest mean |C| "
-                  "among blends whose max C is within 5% of blend 0 (= plain)",
-        "warm_iterations": it, "plain_iterations": cfg.solverIterations,
-        "steps_per_s": round(value, 2), "ms_per_step": round(ms / args.steps, 4),
+                  "Jacobi iterations; the fewest iterations (of 1, 2, 3) whose calibrated blend "
+                  "keeps the max density error at or below the plain solver's on the calibration "
+                  "scene (zero tolerance)",
+        "warm_iterations": k, "plain_iterations": plain_it, "network": net is not None,
+        "steps_per_s": round(value, 2), "ms_per_step": round(ms, 4),
         "speedup_vs_plain": round(value / plain_value, 4),
         "gpu_launches_per_step": launches,
+        "training": {"scenes": ["%s (%d particles)" % (t.name, t.n) for t, _ in train_scenes],
+                     "calibration_scene": train_scenes[0][0].name, "rollout_steps": steps,
+                     **report},
         "density_error": {
-            "rollout_steps": steps,
-            "warm": {"max": round(float(e_warm[:, 0].mean()), 5),
-                     "worst": round(float(e_warm[:, 0].max()), 5),
-                     "mean_abs": round(float(e_warm[:, 1].mean()), 5)},
-            "plain": {"max": round(float(e_plain[:, 0].mean()), 5),
-                      "worst": round(float(e_plain[:, 0].max()), 5),
-                      "mean_abs": round(float(e_plain[:, 1].mean()), 5)},
-            "plain_same_iterations": {"max": round(float(e_plain_same[:, 0].mean()), 5),
-                                      "mean_abs": round(float(e_plain_same[:, 1].mean()), 5)},
+            "rollout_steps": steps, "scenes": accuracy(k, net),
             "definition": "per step: max_i max(rho_i/rho0 - 1, 0) and mean_i |rho_i/rho0 - 1| at "
-                          "the step's final positions over its lists; averaged over the rollout",
-        },
-        "training": {"pairs": int(4 * sc.n), "teacher_iterations": teacher, "epochs": 6,
-                     "batch": 65536, "final_loss": round(losses[-1], 5),
-                     "collect_s": round(t1 - t0, 2), "train_s": round(t2 - t1, 2),
-                     "calibrate_s": round(t3 - t2, 2), "blend": net.blend,
-                     "blend_sweep": {str(k): [round(v[0], 5), round(v[1], 5)]
-                                     for k, v in cal.items()},
-                     "data": "seed-1 copy of the workload (evaluation uses seed 0)"},
-        "kernels_us": {k: round(1000.0 * v[1] / max(v[0], 1), 2) for k, v in prof.items()
-                       if k in ("k_features", "k_mlp_forward", "k_search", "k_delta_correct",
-                                "k_density_lambda", "k_delta_final")},
+                          "the step's final positions over its lists; averaged over the rollout"},
+        "train_and_calibrate_s": round(t1 - t0, 2),
     }
+    if net is not None:
+        net.close()
+    if last is not None:  # the k = 3 network, which did not reach the plain max error
+        lk, lnet = last
+        lv, lms, _, lprof = time_solver(lk, lnet)
+        result["best_network_not_qualified"] = {
+            "warm_iterations": lk, "blend": lnet.blend, "steps_per_s": round(lv, 2),
+            "speedup_vs_plain": round(lv / plain_value, 4),
+            "density_error": accuracy(lk, lnet),
+            "kernels_us": {k_: round(1000.0 * v[1] / max(v[0], 1), 2) for k_, v in lprof.items()
+                           if k_ in ("k_mlp_forward", "k_search", "k_delta_correct",
+                                     "k_density_lambda", "k_delta_final")}}
+        prof = lprof
+        lnet.close()
+    result["kernels_us"] = {k_: round(1000.0 * v[1] / max(v[0], 1), 2) for k_, v in prof.items()
+                            if k_ in ("k_mlp_forward", "k_search", "k_delta_correct",
+                                      "k_density_lambda", "k_delta_final")}
+    return result
 
 
 # ---------------------------------------------------------------------------------- batched scenes
@@ -405,7 +514,7 @@ def run_ours(args, sc, cfg, corr):
     ak.load_library()
 
     stream = torch.cuda.Stream()
-    opts = ak.OPT_EXACT_MATH if args.exact else 0
+    opts = (ak.OPT_EXACT_MATH if args.exact else 0) | (ak.OPT_RESIDENT if args.resident else 0)
     solver = PBFSolver(sc.n, cfg, corr, options=opts, stream=stream)
     table_size = solver.stats()["tableSize"]
     host = sc.particles
@@ -413,12 +522,26 @@ def run_ours(args, sc, cfg, corr):
     torch.cuda.synchronize()
     # launch shapes of the pair kernels, chosen by the solver's autotuner on a copy of the records
     solver.attach(as_particle_buffer(buf))
-    pair_blocks = solver.autotune(sc.dt, sc.box_min, sc.box_max, steps=3)
+    if args.pair_blocks:
+        solver.set_pair_blocks([int(b) for b in args.pair_blocks.split(",")])
+        pair_blocks = solver.pair_blocks()
+    else:
+        pair_blocks = solver.autotune(sc.dt, sc.box_min, sc.box_max, steps=3)
 
     def barrier():
         if dist is not None:
             dist.barrier()
 
+    # pre-roll into the developed flow (untimed), then warm-up
+    with torch.cuda.stream(stream):
+        for _ in range(args.preroll):
+            solver.step(buf, sc.dt, sc.box_min, sc.box_max)
+    torch.cuda.synchronize()
+    sc_initial = sc  # the learned warm start keeps its own protocol from rest
+    if args.preroll:
+        # every later leg (end to end, baselines) starts from the same developed state
+        host = buf.cpu().numpy().view(ak.PARTICLE_DTYPE).copy()
+        sc = dataclasses.replace(sc, particles=host)
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             solver.step(buf, sc.dt, sc.box_min, sc.box_max)
@@ -532,14 +655,37 @@ def run_ours(args, sc, cfg, corr):
 
     learned = None
     if not args.no_learned and cfg.solverIterations > args.learned_iterations:
-        learned = run_learned(args, sc, cfg, corr, stream, value / world, ms / args.steps)
+        learned = run_learned(args, sc_initial, cfg, corr, stream, value / world, ms / args.steps,
+                              sc_timed=sc)
+        # what fewer iterations can buy at most: the plain step minus the saved Jacobi iterations
+        # (one density pass and one delta pass each) plus the network and its features
+        t4 = 1000.0 * ms / args.steps
+        it_us = (kernels.get("k_density_lambda", {}).get("us_per_launch", 0.0)
+                 + kernels.get("k_delta_correct", {}).get("us_per_launch", 0.0))
+        net_us = learned["kernels_us"].get("k_mlp_forward", 0.0)
+        learned["budget"] = {
+            "plain_step_us": round(t4, 1), "iteration_us": round(it_us, 1),
+            "network_us": round(net_us, 1),
+            "max_speedup": {str(k): round(t4 / (t4 - (cfg.solverIterations - k) * it_us + net_us), 3)
+                            for k in (1, 2, 3)},
+            "what": "plain step / (plain step - saved iterations x iteration + network): the "
+                    "speedup at k warm iterations if the network's accuracy cost nothing"}
 
-    cpu = None
+    # baseline legs (rank 0 at N=1, after every timed region): the CPU restatement, the error of
+    # one fast step against the FP64 restatement, and the reference's own kernels on this GPU
+    cpu = fp64_error = reference_gpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         # ~10 s of CPU work at 1M on 16 cores (18 steps); larger scenes fall back to a sub-block
         sps, psps, cores, sample = time_oracle(sc, cfg, corr, 18, 30.0)
         cpu = {"value": sps, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
-               "particle_steps_per_s": psps}
+               "particle_steps_per_s": psps,
+               "precision": "fp32: the reference's arithmetic and contractions, restated for the "
+                            "host (OpenMP over particles)",
+               "state": "the timed window's developed flow (after %d pre-roll steps)"
+                        % args.preroll}
+        fp64_error = step_error_vs_fp64(solver, sc, cfg, corr)
+    if rank == 0 and world == 1 and not args.no_reference_gpu:
+        reference_gpu = time_reference_gpu(sc, cfg, corr, value, e2e)
 
     solver.close()
     if rank == 0:
@@ -558,6 +704,10 @@ def run_ours(args, sc, cfg, corr):
                        "math": "exact" if args.exact else "fast",
                        "parallelism": "replicas x%d" % world,
                        "l2": "per-step working set > L2 (no flush)",
+                       "flow_phase": {"preroll_steps": args.preroll,
+                                      "timed_steps": [args.preroll + args.warmup + 1,
+                                                      args.preroll + args.warmup + args.steps],
+                                      "sim_time_s": round((args.preroll + args.warmup) * sc.dt, 3)},
                        "mean_neighbours": round(mean_c, 3),
                        "list_bytes_per_particle": round(list_bytes, 2),
                        "pair_blocks_autotuned": pair_blocks,
@@ -565,6 +715,8 @@ def run_ours(args, sc, cfg, corr):
             "roofline": roofline,
             "fp32": fp32,
             "cpu_baseline": cpu,
+            "fp64_error": fp64_error,
+            "reference_gpu": reference_gpu,
             "e2e": e2e,
             "gpu_launches": launches_per_step * args.steps,
             "clocks": clocks,

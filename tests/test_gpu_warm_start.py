@@ -1,6 +1,8 @@
 """Learned lambda warm start in the step: training-pair capture, training on the GPU with the
-network's own kernels, and what the trained network gains over the plain solver at the same
-number of Jacobi iterations (density-constraint error measured by the solver)."""
+network's own kernels, what the trained network gains over the plain solver at the same number of
+Jacobi iterations, and the fewest warm-started iterations that keep the plain 4-iteration solver's
+max density error on scenes the network was not trained on (density-constraint error measured by
+the solver)."""
 import numpy as np
 import pytest
 
@@ -125,3 +127,42 @@ def test_calibration_on_mean_error_within_max_bound(trained):
     assert cal[b][0] <= bound
     assert all(cal[b][1] <= cal[g][1] for g in cal if cal[g][0] <= bound)
     net.set_blend(before)
+
+
+def test_equal_max_error_iteration_count(cuda_lib):
+    """The equal-error protocol: networks trained on pairs from dam breaks of the benchmark shape
+    and of the batched family (other block shapes, boxes and gravities); the fewest warm-started
+    iterations (1, 2 or 3) whose blend, calibrated with zero tolerance on the benchmark-shape
+    scene, keeps the max density error at or below the plain 4-iteration solver's.  On scenes not
+    trained on (another seed of that shape, and dam breaks of the batched family from another
+    seed) the chosen count's max error must stay at or below the plain 4-iteration solver's."""
+    from akuaengine_gb300.warm_start import fewest_iterations_at_equal_error, rollout_errors
+
+    cfg, corr = scene.benchmark_params()
+    train_scenes = [(scene.workload("dam_break_27k", seed=0), cfg)] + _family(cfg, seed=5, count=3)
+    k, net, report = fewest_iterations_at_equal_error(train_scenes, corr, candidates=(1, 2, 3),
+                                                      steps=60)
+    print("chosen warm iterations:", k, report)
+    try:
+        held_out = [(scene.workload("dam_break_27k", seed=1), cfg)] + _family(cfg, seed=11, count=2)
+        for sc, c in held_out:
+            plain = rollout_errors(sc, c, corr, cfg.solverIterations, None, 60)
+            warm = rollout_errors(sc, c, corr, k, net, 60)
+            print("%s: warm(%d) max %.5f mean %.5f | plain(4) max %.5f mean %.5f"
+                  % (sc.name, k, warm[:, 0].mean(), warm[:, 1].mean(), plain[:, 0].mean(),
+                     plain[:, 1].mean()))
+            assert warm[:, 0].mean() <= plain[:, 0].mean()
+    finally:
+        if net is not None:
+            net.close()
+
+
+def _family(cfg, seed, count):
+    """The `count` largest dam breaks of a batched-family draw, each with its own gravity."""
+    from akuaengine_gb300 import PBFConfig
+
+    batch = scene.batched_dam_breaks(count=32, seed=seed)
+    order = np.argsort([-d["numParticles"] for d in batch.scenes])[:count]
+    return [(batch.scene(int(k)),
+             PBFConfig(**{**cfg.__dict__, "gravity": tuple(batch.scenes[int(k)]["gravity"])}))
+            for k in order]
