@@ -275,21 +275,25 @@ def calibrate_blend(net: LambdaNet, sc, cfg, corr, iterations: int,
     return res
 
 
-def calibrate_equal_error(net: LambdaNet, sc, cfg, corr, iterations: int, target_max: float,
+def calibrate_equal_error(net: LambdaNet, scenes, corr, iterations: int, targets,
                           blends=(0.25, 0.5, 0.75, 1.0), steps: int = 60, stream=None):
-    """Zero-tolerance calibration against a plain solver's max error: rolls `sc` out with each
-    blend at `iterations` warm-started iterations and keeps the blends whose max density error
-    (mean over the rollout of the per-step max) is at most `target_max`.  Sets and returns the
-    one of them with the lowest mean |C|, or None (blend left at 0) when none qualifies; also
-    returns {blend: (max C, mean |C|)}."""
+    """Zero-tolerance calibration against a plain solver's max error on several scenes: rolls
+    each (scene, config) of `scenes` out with each blend at `iterations` warm-started iterations
+    and keeps the blends whose max density error (mean over the rollout of the per-step max) is at
+    most that scene's entry of `targets` on every scene.  Sets and returns the one of them with the
+    lowest mean |C| summed over the scenes, or None (blend left at 0) when none qualifies; also
+    returns {blend: [(max C, mean |C|) per scene]}."""
     res = {}
     for g in blends:
         net.set_blend(float(g))
-        e = rollout_errors(sc, cfg, corr, iterations, net, steps, stream)
-        res[float(g)] = ((float(e[:, 0].mean()), float(e[:, 1].mean()))
-                         if np.isfinite(e).all() else (float("inf"), float("inf")))
-    ok = [g for g in res if res[g][0] <= target_max]
-    best = min(ok, key=lambda g: (res[g][1], res[g][0])) if ok else None
+        per = []
+        for sc, cfg in scenes:
+            e = rollout_errors(sc, cfg, corr, iterations, net, steps, stream)
+            per.append((float(e[:, 0].mean()), float(e[:, 1].mean()))
+                       if np.isfinite(e).all() else (float("inf"), float("inf")))
+        res[float(g)] = per
+    ok = [g for g in res if all(m <= t for (m, _), t in zip(res[g], targets))]
+    best = min(ok, key=lambda g: sum(v[1] for v in res[g])) if ok else None
     net.set_blend(best if best is not None else 0.0)
     return best, res
 
@@ -309,24 +313,27 @@ def collect_mixed(scenes, corr, teacher_iterations: int, stream=None, collect=No
     return torch.cat(xs), torch.cat(ys)
 
 
-def fewest_iterations_at_equal_error(train_scenes, corr, *, plain_iterations: int = 4,
-                                     candidates=(1, 2, 3), steps: int = 60, stream=None,
-                                     collect=None, epochs: int = 6, batch: int = 65536,
-                                     blends=(0.25, 0.5, 0.75, 1.0), seed: int = 0,
-                                     keep_last: bool = False):
-    """The learned warm start at equal max error.  `train_scenes`: list of (scene, config); the
-    first is also the calibration scene.  For k = candidates in increasing order, trains a network
-    whose target is the lambda sum of a (plain_iterations - k + 1)-iteration teacher (the learned
-    first iteration stands in for the plain iterations it saves) on pairs from every training
-    scene, calibrates its blend with zero tolerance against the plain solver's max error on the
-    calibration scene, and stops at the first k that reaches it.  Returns (k, net or None, report);
-    k = plain_iterations and no network when no candidate qualifies (with `keep_last`, the last
-    candidate's network, blend set to its lowest-max-error blend, is returned as report["last"]
-    for timing and reporting)."""
-    cal_sc, cal_cfg = train_scenes[0]
-    plain = rollout_errors(cal_sc, cal_cfg, corr, plain_iterations, None, steps, stream)
-    target = float(plain[:, 0].mean())
-    report = {"plain_max": target, "plain_mean_abs": float(plain[:, 1].mean()), "tried": {}}
+def fewest_iterations_at_equal_error(train_scenes, corr, *, calibration_scenes=None,
+                                     plain_iterations: int = 4, candidates=(1, 2, 3),
+                                     steps: int = 60, stream=None, collect=None, epochs: int = 6,
+                                     batch: int = 65536, blends=(0.25, 0.5, 0.75, 1.0),
+                                     seed: int = 0, keep_last: bool = False):
+    """The learned warm start at equal max error.  `train_scenes` and `calibration_scenes`: lists
+    of (scene, config) (calibration defaults to the training scenes).  For k = candidates in
+    increasing order, trains a network whose target is the lambda sum of a
+    (plain_iterations - k + 1)-iteration teacher (the learned first iteration stands in for the
+    plain iterations it saves) on pairs from every training scene, calibrates its blend with zero
+    tolerance against the plain solver's max error on every calibration scene, and stops at the
+    first k that reaches it.  Returns (k, net or None, report); k = plain_iterations and no
+    network when no candidate qualifies (with `keep_last`, the last candidate's network, blend set
+    to the blend with the lowest worst-scene max error, is returned as report["last"])."""
+    cal = calibration_scenes or train_scenes
+    targets, plain_means = [], []
+    for sc, cfg in cal:
+        plain = rollout_errors(sc, cfg, corr, plain_iterations, None, steps, stream)
+        targets.append(float(plain[:, 0].mean()))
+        plain_means.append(float(plain[:, 1].mean()))
+    report = {"plain_max": targets, "plain_mean_abs": plain_means, "tried": {}}
     ks = sorted(candidates)
     for k in ks:
         teacher = plain_iterations - k + 1
@@ -336,15 +343,14 @@ def fewest_iterations_at_equal_error(train_scenes, corr, *, plain_iterations: in
         train(net, x, y, epochs=epochs, batch=batch, stream=stream)
         pairs = int(x.shape[0])
         del x, y
-        best, res = calibrate_equal_error(net, cal_sc, cal_cfg, corr, k, target, blends, steps,
-                                          stream)
+        best, res = calibrate_equal_error(net, cal, corr, k, targets, blends, steps, stream)
         report["tried"][str(k)] = {"teacher_iterations": teacher, "blend": best, "pairs": pairs,
-                                   "blends": {str(g): [round(v[0], 5), round(v[1], 5)]
+                                   "blends": {str(g): [[round(a, 5), round(b, 5)] for a, b in v]
                                               for g, v in res.items()}}
         if best is not None:
             return k, net, report
         if keep_last and k == ks[-1]:
-            net.set_blend(min(res, key=lambda g: res[g][0]))
+            net.set_blend(min(res, key=lambda g: max(m / t for (m, _), t in zip(res[g], targets))))
             report["last"] = (k, net)
         else:
             net.close()

@@ -93,6 +93,8 @@ def parse_args(argv=None):
     ap.add_argument("--pair-blocks", default=None,
                     help="six comma-separated block sizes of the pair kernels instead of the "
                          "autotuner's choice (profiling runs)")
+    ap.add_argument("--table-size", type=int, default=None,
+                    help="hash table buckets (default: the reference's maxNeighbours * N)")
     ap.add_argument("--resident", action="store_true",
                     help="records read only on the first step (the key kernel replaces the import "
                          "on later steps)")
@@ -176,14 +178,15 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------------- oracle arm
-def time_oracle(sc, cfg, corr, steps, budget_s, threads=0):
+def time_oracle(sc, cfg, corr, steps, budget_s, threads=0, table_size=None):
     """Times the CPU restatement on `steps` steps, on a sub-block when the full scene would take
     longer than `budget_s`.  Returns (steps/s at full size, cores, sample description)."""
     import numpy as np
 
     import oracle
 
-    P = oracle.make_params(cfg, corr, sc.dt, sc.box_min, sc.box_max, n=sc.n, num_threads=threads)
+    P = oracle.make_params(cfg, corr, sc.dt, sc.box_min, sc.box_max, n=sc.n, num_threads=threads,
+                           table_size=table_size)
     cores = threads if threads > 0 else oracle.max_threads()
     p = sc.particles.copy()
     t0 = time.perf_counter()
@@ -196,7 +199,9 @@ def time_oracle(sc, cfg, corr, steps, budget_s, threads=0):
         n_sample = max(int(sc.n * frac), 4096)
         parts = p[:n_sample].copy()  # a contiguous slab of the hash-sorted particle set
         P = oracle.make_params(cfg, corr, sc.dt, sc.box_min, sc.box_max, n=n_sample,
-                               num_threads=threads)
+                               num_threads=threads,
+                               table_size=None if table_size is None else
+                               max(1, int(table_size * n_sample / sc.n)))
         oracle.step(parts, P)
     t0 = time.perf_counter()
     for _ in range(steps):
@@ -208,7 +213,7 @@ def time_oracle(sc, cfg, corr, steps, budget_s, threads=0):
     return psps / sc.n, psps, cores, sample
 
 
-def step_error_vs_fp64(solver, sc, cfg, corr):
+def step_error_vs_fp64(solver, sc, cfg, corr, table_size=None):
     """One fast-math GPU step of the scene's state against the same step of the restatement in
     FP64 and in FP32 (the checker; outside every timed region): per-particle position error
     quantiles, so the GPU's error is read against the FP32 arithmetic's own."""
@@ -222,7 +227,7 @@ def step_error_vs_fp64(solver, sc, cfg, corr):
     for name, flags in (("fp32_oracle", oracle.FMA), ("fp64_oracle", oracle.FMA | oracle.FP64)):
         p = sc.particles.copy()
         oracle.step(p, oracle.make_params(cfg, corr, sc.dt, sc.box_min, sc.box_max, n=sc.n,
-                                          flags=flags))
+                                          flags=flags, table_size=table_size))
         out[name] = p
     def q(a, b):
         d = np.abs(a["position"].astype(np.float64) - b["position"]).max(axis=1)
@@ -235,7 +240,7 @@ def step_error_vs_fp64(solver, sc, cfg, corr):
                     "max over x, y, z"}
 
 
-def time_reference_gpu(sc, cfg, corr, value, e2e):
+def time_reference_gpu(sc, cfg, corr, value, e2e, table_size=None):
     """The reference's unchanged CUDA kernels (compiled from its sources into cubins, driven by a
     re-sequenced PBFSolver::step) on this GPU and the same state: the faithful form (host-resident
     neighbour lists, per-step table allocation, as the reference's wrappers do) and the form with
@@ -256,6 +261,8 @@ def time_reference_gpu(sc, cfg, corr, value, e2e):
         for mode, steps in (("faithful", 10), ("resident", 20)):
             p = sc.particles.copy()
             pr = params(cfg, corr, sc, sc.n)
+            if table_size:
+                pr["table"] = int(table_size)
             pr["warmup"] = 1
             info = ref_gpu.run(p, pr, steps, mode=mode)
             v = 1000.0 / info["ms_per_step"]
@@ -279,7 +286,8 @@ def run_reference(args, sc, cfg, corr):
     budget = 150.0
     per_step_budget = budget / max(args.steps, 1)
     # warm-up: W steps of a small sample (the oracle has no caches to warm beyond the first call)
-    sps, psps, cores, sample = time_oracle(sc, cfg, corr, args.steps, budget)
+    sps, psps, cores, sample = time_oracle(sc, cfg, corr, args.steps, budget,
+                                           table_size=args.table_size)
     line = {
         "impl": "reference", "metric": WORKLOADS[args.workload][0], "value": sps, "unit": UNIT,
         "n_gpus": args.gpus,
@@ -321,8 +329,8 @@ def run_learned(args, sc, cfg, corr, stream, plain_value, plain_ms, sc_timed=Non
     family (other block shapes, boxes and gravities).  For k = 1, 2, 3 warm-started iterations
     (fewest first) a network is trained on a teacher of 4 - k + 1 plain iterations (the learned
     first iteration stands in for the iterations it saves) and its blend is calibrated on the
-    workload copy with zero tolerance against the plain solver's max error; the first k that
-    reaches it is the equal-error result.  Reported beside it: the k = 3 network timed and
+    training scenes with zero tolerance against the plain solver's max error on each; the first k
+    that reaches it is the equal-error result.  Reported beside it: the k = 3 network timed and
     evaluated whether or not it qualified.  Steps are device-timed like the main line, from the
     same state; errors come from scenes not trained on (the benchmark scene, and a batched-family
     scene of another draw)."""
@@ -333,7 +341,7 @@ def run_learned(args, sc, cfg, corr, stream, plain_value, plain_ms, sc_timed=Non
     from akuaengine_gb300.warm_start import fewest_iterations_at_equal_error, rollout_errors
 
     t0 = time.perf_counter()
-    train_scenes = [(scene.workload(args.workload, seed=1), cfg)] + _family(cfg, 3, 8)
+    train_scenes = [(scene.workload(args.workload, seed=1), cfg)] + _family(cfg, 3, 4)
     plain_it = cfg.solverIterations
     steps = 60
     k, net, report = fewest_iterations_at_equal_error(
@@ -400,8 +408,9 @@ def run_learned(args, sc, cfg, corr, stream, plain_value, plain_ms, sc_timed=Non
         "speedup_vs_plain": round(value / plain_value, 4),
         "gpu_launches_per_step": launches,
         "training": {"scenes": ["%s (%d particles)" % (t.name, t.n) for t, _ in train_scenes],
-                     "calibration_scene": train_scenes[0][0].name, "rollout_steps": steps,
-                     **report},
+                     "calibration": "zero tolerance against the plain solver's max error on every "
+                                    "training scene",
+                     "rollout_steps": steps, **report},
         "density_error": {
             "rollout_steps": steps, "scenes": accuracy(k, net),
             "definition": "per step: max_i max(rho_i/rho0 - 1, 0) and mean_i |rho_i/rho0 - 1| at "
@@ -515,7 +524,7 @@ def run_ours(args, sc, cfg, corr):
 
     stream = torch.cuda.Stream()
     opts = (ak.OPT_EXACT_MATH if args.exact else 0) | (ak.OPT_RESIDENT if args.resident else 0)
-    solver = PBFSolver(sc.n, cfg, corr, options=opts, stream=stream)
+    solver = PBFSolver(sc.n, cfg, corr, options=opts, stream=stream, table_size=args.table_size)
     table_size = solver.stats()["tableSize"]
     host = sc.particles
     buf = torch.from_numpy(host.view(np.uint8).copy()).cuda()
@@ -676,16 +685,16 @@ def run_ours(args, sc, cfg, corr):
     cpu = fp64_error = reference_gpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         # ~10 s of CPU work at 1M on 16 cores (18 steps); larger scenes fall back to a sub-block
-        sps, psps, cores, sample = time_oracle(sc, cfg, corr, 18, 30.0)
+        sps, psps, cores, sample = time_oracle(sc, cfg, corr, 18, 30.0, table_size=args.table_size)
         cpu = {"value": sps, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
                "particle_steps_per_s": psps,
                "precision": "fp32: the reference's arithmetic and contractions, restated for the "
                             "host (OpenMP over particles)",
                "state": "the timed window's developed flow (after %d pre-roll steps)"
                         % args.preroll}
-        fp64_error = step_error_vs_fp64(solver, sc, cfg, corr)
+        fp64_error = step_error_vs_fp64(solver, sc, cfg, corr, args.table_size)
     if rank == 0 and world == 1 and not args.no_reference_gpu:
-        reference_gpu = time_reference_gpu(sc, cfg, corr, value, e2e)
+        reference_gpu = time_reference_gpu(sc, cfg, corr, value, e2e, args.table_size)
 
     solver.close()
     if rank == 0:

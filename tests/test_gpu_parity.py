@@ -341,13 +341,16 @@ def test_fast_one_step_1m_full_size():
     assert_close_fast(g, o)
 
 
-def test_exact_one_step_8m_double_dam_break():
-    """8M particles in two blocks (the table is 128 N = 1.024e9 buckets, as the reference's
-    formula gives): one step, grid and every record bit-exact against the oracle."""
+@pytest.mark.parametrize("table_size", [None, 1 << 24], ids=["table_128N", "table_2e24"])
+def test_exact_one_step_8m_double_dam_break(table_size):
+    """8M particles in two blocks, with the reference's table of 128 N = 1.024e9 buckets and with
+    the 2^24-bucket table of the 8M workload (about 61 particles per bucket on average, so most
+    buckets hold several cells): one step, grid and every record bit-exact against the oracle at
+    the same table size."""
     sc = scene.workload("double_dam_break_8m", seed=0)
     cfg, corr = bench_params()
-    g, ge = run_gpu(sc, cfg, corr, 1, ak.OPT_EXACT_MATH)
-    o, oe = run_oracle(sc, cfg, corr, 1)
+    g, ge = run_gpu(sc, cfg, corr, 1, ak.OPT_EXACT_MATH, table_size=table_size)
+    o, oe = run_oracle(sc, cfg, corr, 1, table_size=table_size)
     assert_grid_equal(ge, oe, cfg.maxNeighbours)
     assert_records_bitexact(g, o)
 

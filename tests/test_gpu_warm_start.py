@@ -132,16 +132,18 @@ def test_calibration_on_mean_error_within_max_bound(trained):
 def test_equal_max_error_iteration_count(cuda_lib):
     """The equal-error protocol: networks trained on pairs from dam breaks of the benchmark shape
     and of the batched family (other block shapes, boxes and gravities); the fewest warm-started
-    iterations (1, 2 or 3) whose blend, calibrated with zero tolerance on the benchmark-shape
-    scene, keeps the max density error at or below the plain 4-iteration solver's.  On scenes not
-    trained on (another seed of that shape, and dam breaks of the batched family from another
-    seed) the chosen count's max error must stay at or below the plain 4-iteration solver's."""
+    iterations (1, 2 or 3) whose blend, calibrated with zero tolerance on all of those scenes,
+    keeps the max density error at or below the plain 4-iteration solver's on each (with no such
+    count the plain solver is the result, k = 4).  On scenes not trained on (another seed of the
+    benchmark shape, and dam breaks of the batched family from another draw) the chosen count's
+    max error must stay at or below the plain 4-iteration solver's."""
     from akuaengine_gb300.warm_start import fewest_iterations_at_equal_error, rollout_errors
 
     cfg, corr = scene.benchmark_params()
     train_scenes = [(scene.workload("dam_break_27k", seed=0), cfg)] + _family(cfg, seed=5, count=3)
     k, net, report = fewest_iterations_at_equal_error(train_scenes, corr, candidates=(1, 2, 3),
                                                       steps=60)
+    assert 1 <= k <= cfg.solverIterations
     print("chosen warm iterations:", k, report)
     try:
         held_out = [(scene.workload("dam_break_27k", seed=1), cfg)] + _family(cfg, seed=11, count=2)
