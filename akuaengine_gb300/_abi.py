@@ -164,6 +164,9 @@ _SIGS = {
     "akua_pbf_set_solver_iterations": (ctypes.c_int, [_P, ctypes.c_int32]),
     "akua_pbf_set_pair_blocks": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int32)]),
     "akua_pbf_get_pair_blocks": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int32)]),
+    "akua_pbf_set_search_shape": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32]),
+    "akua_pbf_get_search_shape": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int32),
+                                                 ctypes.POINTER(ctypes.c_int32)]),
     "akua_pbf_autotune": (ctypes.c_int, [_P, ctypes.c_float, _P, _P, ctypes.c_int32,
                                          ctypes.POINTER(ctypes.c_int32)]),
     "akua_pbf_set_sdf_shapes": (ctypes.c_int, [_P, ctypes.POINTER(CSdfShape), ctypes.c_int32,

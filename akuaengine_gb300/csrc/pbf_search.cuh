@@ -23,10 +23,11 @@
 // per round (independent ballots and placements, distances in packed FP32x2): their dependency
 // chains interleave, which a lane-serial walk or a windowed one (both measured slower) cannot.
 //
-// The first kListStage entries of each list are staged in shared memory and written out as
-// coalesced uint4 tiles (pbf_pairs.cuh).  When `density` is set, the first Jacobi iteration's
-// density and lambda are accumulated over the finished list, one thread per particle (same terms,
-// same order as k_density_lambda).
+// The first STAGE entries of each list are staged in shared memory and written out as coalesced
+// uint4 tiles (pbf_pairs.cuh).  The block size and STAGE (the walk's tile shape) are template
+// parameters; the solver's autotuner picks them by measurement (lists do not depend on them).
+// When `density` is set, the first Jacobi iteration's density and lambda are accumulated over the
+// finished list, one thread per particle (same terms, same order as k_density_lambda).
 #pragma once
 
 #include <cstdint>
@@ -38,17 +39,21 @@
 
 namespace akua {
 
-constexpr int kSearchBlock = 128;
-constexpr int kListStage = 32;            // list entries staged per particle
-constexpr int kListRow = kListStage + 4;  // row stride in words: 9 x 16 B, conflict-free uint4 rows
-constexpr size_t kSearchSmem =
-    sizeof(uint32_t) * kSearchBlock * kListRow + sizeof(float4) * kSearchBlock;
+constexpr int kSearchBlock = 128;  // default tile shape: 128 threads, 32 staged entries
+constexpr int kListStage = 32;
+// Row stride in words of STAGE staged entries: STAGE + 4 words, an odd number of 16-byte units
+// (9 for 32, 5 for 16), so the uint4 rows of a warp's lanes fall in different banks.
+__host__ __device__ constexpr int list_row(int stage) { return stage + 4; }
+__host__ __device__ constexpr size_t search_smem(int block, int stage) {
+    return sizeof(uint32_t) * block * list_row(stage) + sizeof(float4) * block;
+}
+constexpr size_t kSearchSmem = search_smem(kSearchBlock, kListStage);
 constexpr uint32_t kFullWarp = 0xffffffffu;
 constexpr uint32_t kMixedBucket = 0x80000000u;  // bucket table: y bit for a mixed bucket
 constexpr uint32_t kDenseRun = 2048;  // candidates of a run beyond which the walk may stop early
 
-template <bool EXACT>
-__global__ void __launch_bounds__(kSearchBlock)
+template <bool EXACT, int BLOCK, int STAGE>
+__global__ void __launch_bounds__(BLOCK)
     k_search(const StepParams* __restrict__ P, const float4* __restrict__ ps,
              const float4* __restrict__ xref, const uint2* __restrict__ table,
              const uint32_t* __restrict__ r2i, uint32_t* __restrict__ nbr,
@@ -61,11 +66,12 @@ __global__ void __launch_bounds__(kSearchBlock)
     const int n = p.n;
     const int lane = threadIdx.x & 31;
     const int wbase = threadIdx.x & ~31;
-    const int base = blockIdx.x * kSearchBlock + wbase;  // this warp's first particle
+    constexpr int kListRow = list_row(STAGE);
+    const int base = blockIdx.x * BLOCK + wbase;  // this warp's first particle
     if (base >= n) return;                               // uniform over the warp
     const int i = base + lane;
     const bool valid = i < n;
-    float4* xs = reinterpret_cast<float4*>(stage + kSearchBlock * kListRow) + wbase;
+    float4* xs = reinterpret_cast<float4*>(stage + BLOCK * kListRow) + wbase;
     uint32_t* rows = stage + wbase * kListRow;
 
     const float4 xi = valid ? ps[i] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -140,7 +146,7 @@ __global__ void __launch_bounds__(kSearchBlock)
             const uint32_t jrel = j - (uint32_t)base;  // == q for particle q's own slot
             const float2 cxx = f2(c.x), cyy = f2(c.y), czz = f2(c.z);
             auto place = [&](int q, int pos) {
-                if (pos < kListStage) rows[q * kListRow + pos] = j;
+                if (pos < STAGE) rows[q * kListRow + pos] = j;
                 else if (pos < cap) nbr[4 * ((size_t)(pos >> 2) * n + base + q) + (pos & 3)] = j;
             };
             int q = q0;
@@ -192,7 +198,7 @@ __global__ void __launch_bounds__(kSearchBlock)
     const uint32_t* myrow = rows + lane * kListRow;
 
     // staged entries -> global tiles (a partial last tile carries unused words)
-    const int staged = min(count, kListStage);
+    const int staged = min(count, STAGE);
     const uint4* row4 = reinterpret_cast<const uint4*>(myrow);
     uint4* out4 = reinterpret_cast<uint4*>(nbr);
     for (int g = 0; g < (staged + 3) >> 2; ++g) out4[(size_t)g * n + i] = row4[g];
@@ -204,7 +210,7 @@ __global__ void __launch_bounds__(kSearchBlock)
         acc.init(xi.w, p);
         const uint4* tiles = reinterpret_cast<const uint4*>(nbr) + i;
         for (int g = 0; 4 * g < count; ++g) {
-            const uint4 e = g < kListStage / 4 ? row4[g] : tiles[(size_t)g * n];
+            const uint4 e = g < STAGE / 4 ? row4[g] : tiles[(size_t)g * n];
             const int left = count - 4 * g;
             acc.add2(p, xi, __ldg(ps + e.x), __ldg(ps + (left >= 2 ? e.y : e.x)), left >= 2);
             if (left > 2)

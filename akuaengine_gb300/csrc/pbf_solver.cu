@@ -110,6 +110,9 @@ struct akua_pbf {
 
     // block sizes of the neighbour-pair kernels (akua_pbf_set_pair_blocks / akua_pbf_autotune)
     int pair_block[AKUA_PBF_PAIR_KERNELS] = {128, 128, 128, 128, 128, 128};
+    // the walk's tile shape (akua_pbf_set_search_shape / akua_pbf_autotune)
+    int search_block = akua::kSearchBlock;
+    int search_stage = akua::kListStage;
 
     int64_t steps = 0;
     uint64_t device_bytes = 0;
@@ -312,6 +315,29 @@ struct Marker {
     }
 };
 
+// The walk at one tile shape (BLOCK threads, STAGE staged list entries per particle).
+template <bool EXACT, int BLOCK, int STAGE>
+void launch_search_shape(akua_pbf* s, cudaStream_t st, int density, float* feat) {
+    akua::k_search<EXACT, BLOCK, STAGE><<<grid_for(s->n, BLOCK), BLOCK,
+                                          akua::search_smem(BLOCK, STAGE), st>>>(
+        s->d_params, s->ps0, s->xref, s->table, s->r2i, s->nbr, s->cnt, s->rho, s->lam,
+        s->flags, density, s->speed, s->lprev, s->lacc, feat, s->psl);
+}
+
+template <bool EXACT>
+void launch_search(akua_pbf* s, cudaStream_t st, int density, float* feat) {
+    const int b = s->search_block, g = s->search_stage;
+    if (g == 16) {
+        if (b == 64) launch_search_shape<EXACT, 64, 16>(s, st, density, feat);
+        else if (b == 256) launch_search_shape<EXACT, 256, 16>(s, st, density, feat);
+        else launch_search_shape<EXACT, 128, 16>(s, st, density, feat);
+    } else {
+        if (b == 64) launch_search_shape<EXACT, 64, 32>(s, st, density, feat);
+        else if (b == 256) launch_search_shape<EXACT, 256, 32>(s, st, density, feat);
+        else launch_search_shape<EXACT, 128, 32>(s, st, density, feat);
+    }
+}
+
 template <bool EXACT>
 void enqueue_pairs(akua_pbf* s, cudaStream_t st, Marker& mark) {
     const int n = s->n;
@@ -321,11 +347,7 @@ void enqueue_pairs(akua_pbf* s, cudaStream_t st, Marker& mark) {
     float4* ps[2] = {s->ps0, s->ps1};
     const uint4* nbr4 = reinterpret_cast<const uint4*>(s->nbr);
     const int learn = learn_mode(s);
-    akua::k_search<EXACT><<<grid_for(n, akua::kSearchBlock), akua::kSearchBlock,
-                            akua::kSearchSmem, st>>>(
-        s->d_params, s->ps0, s->xref, s->table, s->r2i, s->nbr, s->cnt, s->rho, s->lam,
-        s->flags, iters > 0 ? 1 : 0, s->speed, s->lprev, s->lacc, learn ? s->feat : nullptr,
-        s->psl);
+    launch_search<EXACT>(s, st, iters > 0 ? 1 : 0, learn ? s->feat : nullptr);
     mark("k_search");
     if (learn == 2) {
         akua::mlp::enqueue_forward(s->warm, s->feat, n, s->lam, s->lacc, &s->psl->w, st);
@@ -649,13 +671,8 @@ int create_solver(int32_t n, const akua_pbf_config* cfg, const akua_lambda_corr_
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->side_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming);
-    // the staged neighbour walk needs more than the default 48 KB of dynamic shared memory
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(akua::k_search<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)akua::kSearchSmem);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(akua::k_search<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)akua::kSearchSmem);
+    // every tile shape of the walk fits the default 48 KB of dynamic shared memory
+    static_assert(akua::search_smem(256, 32) <= 48 * 1024, "walk staging exceeds 48 KB");
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
         free_all(s);
@@ -1065,6 +1082,22 @@ int akua_pbf_get_pair_blocks(akua_pbf* s, int32_t blocks[AKUA_PBF_PAIR_KERNELS])
     return AKUA_OK;
 }
 
+int akua_pbf_set_search_shape(akua_pbf* s, int32_t block, int32_t staged) {
+    if (!s || (block != 64 && block != 128 && block != 256) || (staged != 16 && staged != 32))
+        return AKUA_ERR_INVALID_ARGUMENT;
+    s->search_block = block;
+    s->search_stage = staged;
+    invalidate_graph(s);
+    return AKUA_OK;
+}
+
+int akua_pbf_get_search_shape(akua_pbf* s, int32_t* block, int32_t* staged) {
+    if (!s || !block || !staged) return AKUA_ERR_INVALID_ARGUMENT;
+    *block = s->search_block;
+    *staged = s->search_stage;
+    return AKUA_OK;
+}
+
 int akua_pbf_autotune(akua_pbf* s, float dt, const float bmin[3], const float bmax[3],
                       int32_t steps, int32_t* blocks_out) {
     if (!s || steps <= 0 || steps > 100) return AKUA_ERR_INVALID_ARGUMENT;
@@ -1096,8 +1129,9 @@ int akua_pbf_autotune(akua_pbf* s, float dt, const float bmin[3], const float bm
         choice[k] = s->pair_block[k];
     }
     std::vector<akua_kernel_time> times(64);
-    for (int c = 0; c < 3 && rc == AKUA_OK; ++c) {
-        for (int k = 0; k < AKUA_PBF_PAIR_KERNELS; ++k) s->pair_block[k] = cands[c];
+    int32_t count = 0;
+    // one timed trial of the current launch shapes from a copy of the user's records
+    auto trial = [&]() {
         invalidate_graph(s);
         // every candidate starts from the same records (and lambda sums)
         e = cudaMemcpy(tmp, user, bytes, cudaMemcpyDeviceToDevice);
@@ -1109,19 +1143,45 @@ int akua_pbf_autotune(akua_pbf* s, float dt, const float bmin[3], const float bm
         if (rc == AKUA_OK) rc = akua_pbf_profile_begin(s, steps);
         for (int k = 0; k < steps && rc == AKUA_OK; ++k)
             rc = do_step(s, tmp, s->stride, false, dt, bmin, bmax);
-        int32_t count = 0;
+        count = 0;
         const int rc_end = akua_pbf_profile_end(s, times.data(), (int32_t)times.size(), &count);
         if (rc == AKUA_OK) rc = rc_end;
-        for (int t = 0; t < count && rc == AKUA_OK; ++t)
-            for (int k = 0; k < AKUA_PBF_PAIR_KERNELS; ++k)
-                if (std::strcmp(times[t].name, names[k]) == 0 && times[t].launches > 0) {
-                    const double per = times[t].total_ms / times[t].launches;
-                    if (per < best[k]) {
-                        best[k] = per;
-                        choice[k] = cands[c];
-                    }
-                }
+    };
+    auto per_launch = [&](const char* name) {
+        for (int t = 0; t < count; ++t)
+            if (std::strcmp(times[t].name, name) == 0 && times[t].launches > 0)
+                return times[t].total_ms / times[t].launches;
+        return 1e30;
+    };
+    for (int c = 0; c < 3 && rc == AKUA_OK; ++c) {
+        for (int k = 0; k < AKUA_PBF_PAIR_KERNELS; ++k) s->pair_block[k] = cands[c];
+        trial();
+        for (int k = 0; k < AKUA_PBF_PAIR_KERNELS && rc == AKUA_OK; ++k) {
+            const double per = per_launch(names[k]);
+            if (per < best[k]) {
+                best[k] = per;
+                choice[k] = cands[c];
+            }
+        }
     }
+    // the walk's tile shape, with the pair kernels at their chosen sizes
+    for (int k = 0; k < AKUA_PBF_PAIR_KERNELS; ++k) s->pair_block[k] = choice[k];
+    const int shapes[6][2] = {{128, 32}, {64, 32}, {256, 32}, {128, 16}, {64, 16}, {256, 16}};
+    int shape_choice[2] = {s->search_block, s->search_stage};
+    double shape_best = 1e30;
+    for (int c = 0; c < 6 && rc == AKUA_OK; ++c) {
+        s->search_block = shapes[c][0];
+        s->search_stage = shapes[c][1];
+        trial();
+        const double per = per_launch("k_search");
+        if (rc == AKUA_OK && per < shape_best) {
+            shape_best = per;
+            shape_choice[0] = shapes[c][0];
+            shape_choice[1] = shapes[c][1];
+        }
+    }
+    s->search_block = shape_choice[0];
+    s->search_stage = shape_choice[1];
     for (int k = 0; k < AKUA_PBF_PAIR_KERNELS; ++k) {
         s->pair_block[k] = choice[k];
         if (blocks_out) blocks_out[k] = choice[k];

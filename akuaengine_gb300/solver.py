@@ -184,9 +184,21 @@ class PBFSolver:
         b = (ctypes.c_int32 * 6)(*[int(x) for x in blocks])
         check(self._lib.akua_pbf_set_pair_blocks(self._h, b), "akua_pbf_set_pair_blocks")
 
+    def search_shape(self) -> tuple[int, int]:
+        """The neighbour walk's tile shape: (block size, staged list entries per particle)."""
+        b, g = ctypes.c_int32(), ctypes.c_int32()
+        check(self._lib.akua_pbf_get_search_shape(self._h, ctypes.byref(b), ctypes.byref(g)),
+              "akua_pbf_get_search_shape")
+        return b.value, g.value
+
+    def set_search_shape(self, block: int, staged: int) -> None:
+        check(self._lib.akua_pbf_set_search_shape(self._h, int(block), int(staged)),
+              "akua_pbf_set_search_shape")
+
     def autotune(self, deltaTime: float, boxMin=None, boxMax=None, steps: int = 3) -> dict:
-        """Chooses each pair kernel's block size by timing, on a copy of the attached records
-        (attach a buffer first); returns the choice by kernel name."""
+        """Chooses each pair kernel's block size, then the walk's tile shape, by timing, on a copy
+        of the attached records (attach a buffer first); returns the pair kernels' choice by
+        kernel name (the walk's: `search_shape()`)."""
         b = (ctypes.c_int32 * 6)()
         check(self._lib.akua_pbf_autotune(self._h, float(deltaTime),
                                           None if boxMin is None else vec3(boxMin),

@@ -93,6 +93,9 @@ def parse_args(argv=None):
     ap.add_argument("--pair-blocks", default=None,
                     help="six comma-separated block sizes of the pair kernels instead of the "
                          "autotuner's choice (profiling runs)")
+    ap.add_argument("--search-shape", default=None,
+                    help="the walk's block size and staged entries, e.g. 128,32 (with "
+                         "--pair-blocks: profiling runs; default: the autotuner's choice)")
     ap.add_argument("--table-size", type=int, default=None,
                     help="hash table buckets (default: the reference's maxNeighbours * N)")
     ap.add_argument("--resident", action="store_true",
@@ -475,7 +478,24 @@ def run_batched(args, cfg, corr):
     per = np.array([evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)])
     ms = float(per.sum())
     launches = solver.kernels_per_step()
+    search_shape = solver.search_shape()
+    # what launching costs: the same steps with every kernel launched one by one and bracketed
+    # by events (the sum includes each launch's gap) against the graph-launched batch step
+    prof_steps = 5
+    solver.profile_begin(prof_steps)
+    for _ in range(prof_steps):
+        solver.step(buf, b.dt)
+    prof = solver.profile_end()
     solver.close()
+    kernel_sum_ms = sum(v[1] for v in prof.values()) / prof_steps
+    launch_cost = {
+        "launches_per_batch_step": launches,
+        "graph_step_ms": round(ms / args.steps, 4),
+        "kernels_launched_one_by_one_ms": round(kernel_sum_ms, 4),
+        "kernels": {k: round(1000.0 * v[1] / max(v[0], 1), 2) for k, v in prof.items()},
+        "what": "the second figure times each kernel between events with its own launch (sorts "
+                "not overlapped); a persistent kernel could save at most the graph's per-launch "
+                "gaps, launches x about a microsecond"}
     if rank == 0:
         line = {
             "metric": "batched scenes particle-steps/s", "value": round(b.n * args.steps / (ms / 1e3), 1),
@@ -488,7 +508,10 @@ def run_batched(args, cfg, corr):
                                            int(max(d["numParticles"] for d in b.scenes))],
                        "dt": b.dt, "solver_iterations": cfg.solverIterations,
                        "table_size": int(cfg.maxNeighbours * b.n),
-                       "pair_blocks_autotuned": pair_blocks},
+                       "pair_blocks_autotuned": pair_blocks,
+                       "walk_shape_autotuned": {"block": search_shape[0],
+                                                "staged_entries": search_shape[1]}},
+            "launch_cost": launch_cost,
             "batch_step_ms": {"p50": round(float(np.percentile(per, 50)), 4),
                               "p99": round(float(np.percentile(per, 99)), 4),
                               "max": round(float(per.max()), 4)},
@@ -534,8 +557,10 @@ def run_ours(args, sc, cfg, corr):
     if args.pair_blocks:
         solver.set_pair_blocks([int(b) for b in args.pair_blocks.split(",")])
         pair_blocks = solver.pair_blocks()
+        solver.set_search_shape(*[int(v) for v in (args.search_shape or "128,32").split(",")])
     else:
         pair_blocks = solver.autotune(sc.dt, sc.box_min, sc.box_max, steps=3)
+    search_shape = solver.search_shape()
 
     def barrier():
         if dist is not None:
@@ -720,6 +745,8 @@ def run_ours(args, sc, cfg, corr):
                        "mean_neighbours": round(mean_c, 3),
                        "list_bytes_per_particle": round(list_bytes, 2),
                        "pair_blocks_autotuned": pair_blocks,
+                       "walk_shape_autotuned": {"block": search_shape[0],
+                                                "staged_entries": search_shape[1]},
                        "buckets_per_particle": round(buckets_per_particle, 4)},
             "roofline": roofline,
             "fp32": fp32,

@@ -223,11 +223,17 @@ int akua_pbf_set_scene(akua_pbf* solver, int32_t scene, const akua_scene_desc* d
 #define AKUA_PBF_PAIR_KERNELS 6
 int akua_pbf_set_pair_blocks(akua_pbf* solver, const int32_t blocks[AKUA_PBF_PAIR_KERNELS]);
 int akua_pbf_get_pair_blocks(akua_pbf* solver, int32_t blocks[AKUA_PBF_PAIR_KERNELS]);
-/* Autotuner: times every candidate block size of every pair kernel over `steps` profiled steps
- * (after one warm-up step) started from a copy of the attached records, and keeps the fastest per
- * kernel (written to blocksOut when not NULL).  The attached records, the step count, pending
- * captures and the lambda sums are left as they were.  boxMin/boxMax as for akua_pbf_step (NULL
- * for a batch, whose scenes carry their boxes).  Synchronous. */
+/* The neighbour walk's tile shape: its block size (64, 128 or 256 threads) and how many list
+ * entries per particle it stages in shared memory before writing them out (16 or 32); lists do
+ * not depend on it.  Default 128 / 32. */
+int akua_pbf_set_search_shape(akua_pbf* solver, int32_t block, int32_t staged);
+int akua_pbf_get_search_shape(akua_pbf* solver, int32_t* block, int32_t* staged);
+/* Autotuner: times every candidate block size of every pair kernel, then every walk tile shape,
+ * over `steps` profiled steps (after one warm-up step) started from a copy of the attached
+ * records, and keeps the fastest per kernel (the pair kernels' written to blocksOut when not
+ * NULL; the walk's shape read back with akua_pbf_get_search_shape).  The attached records, the
+ * step count, pending captures and the lambda sums are left as they were.  boxMin/boxMax as for
+ * akua_pbf_step (NULL for a batch, whose scenes carry their boxes).  Synchronous. */
 int akua_pbf_autotune(akua_pbf* solver, float deltaTime, const float boxMin[3],
                       const float boxMax[3], int32_t steps, int32_t* blocksOut);
 

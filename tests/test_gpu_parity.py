@@ -341,6 +341,26 @@ def test_fast_one_step_1m_full_size():
     assert_close_fast(g, o)
 
 
+@pytest.mark.parametrize("shape", [(64, 32), (256, 32), (64, 16), (128, 16), (256, 16)])
+def test_walk_tile_shapes_identical(shape):
+    """Every tile shape of the walk the autotuner can pick gives the default shape's records,
+    lists and order bit for bit (three steps, both math modes)."""
+    sc = scene.workload("dam_break_27k", seed=9)
+    cfg, corr = bench_params()
+    for opts in (0, ak.OPT_EXACT_MATH):
+        outs = []
+        for sh in ((128, 32), shape):
+            p = sc.particles.copy()
+            with PBFSolver(sc.n, cfg, corr, options=opts) as s:
+                s.set_search_shape(*sh)
+                assert s.search_shape() == sh
+                for _ in range(3):
+                    s.step_host(p, sc.dt, sc.box_min, sc.box_max)
+                outs.append((p, s.read_debug(ak.DEBUG_NEIGHBOURS), s.read_debug(ak.DEBUG_ORDER)))
+        assert outs[0][0].tobytes() == outs[1][0].tobytes()
+        assert np.array_equal(outs[0][1], outs[1][1]) and np.array_equal(outs[0][2], outs[1][2])
+
+
 @pytest.mark.parametrize("table_size", [None, 1 << 24], ids=["table_128N", "table_2e24"])
 def test_exact_one_step_8m_double_dam_break(table_size):
     """8M particles in two blocks, with the reference's table of 128 N = 1.024e9 buckets and with
