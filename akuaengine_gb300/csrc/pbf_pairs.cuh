@@ -432,8 +432,10 @@ __global__ void __launch_bounds__(kMaxPairBlock)
 
 // Vorticity confinement (IntegrationCUDA.cu:130-165); writes the confined velocity to the
 // particle records (x, m_i / rho_i | v) for the XSPH pass.
+// Capped at 48 registers (five 256-thread blocks per SM): 80 µs against 84 at 60 registers on the
+// 1M scene, although 36 bytes spill; the same cap slowed vorticity and the last delta pass.
 template <bool EXACT>
-__global__ void __launch_bounds__(kMaxPairBlock)
+__global__ void __launch_bounds__(kMaxPairBlock, 5)
     k_confine(const StepParams* __restrict__ P, const float4* __restrict__ x4,
               const float4* __restrict__ v4, const float4* __restrict__ om4,
               const float* __restrict__ rho, const uint4* __restrict__ nbr4,

@@ -327,7 +327,10 @@ void launch_search_shape(akua_pbf* s, cudaStream_t st, int density, float* feat)
 template <bool EXACT>
 void launch_search(akua_pbf* s, cudaStream_t st, int density, float* feat) {
     const int b = s->search_block, g = s->search_stage;
-    if (g == 16) {
+    if (g == 48) {  // 64 or 128 threads (256 x 48 entries would exceed 48 KB of shared memory)
+        if (b == 64) launch_search_shape<EXACT, 64, 48>(s, st, density, feat);
+        else launch_search_shape<EXACT, 128, 48>(s, st, density, feat);
+    } else if (g == 16) {
         if (b == 64) launch_search_shape<EXACT, 64, 16>(s, st, density, feat);
         else if (b == 256) launch_search_shape<EXACT, 256, 16>(s, st, density, feat);
         else launch_search_shape<EXACT, 128, 16>(s, st, density, feat);
@@ -672,7 +675,8 @@ int create_solver(int32_t n, const akua_pbf_config* cfg, const akua_lambda_corr_
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming);
     // every tile shape of the walk fits the default 48 KB of dynamic shared memory
-    static_assert(akua::search_smem(256, 32) <= 48 * 1024, "walk staging exceeds 48 KB");
+    static_assert(akua::search_smem(256, 32) <= 48 * 1024 && akua::search_smem(128, 48) <= 48 * 1024,
+                  "walk staging exceeds 48 KB");
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
         free_all(s);
@@ -1083,7 +1087,8 @@ int akua_pbf_get_pair_blocks(akua_pbf* s, int32_t blocks[AKUA_PBF_PAIR_KERNELS])
 }
 
 int akua_pbf_set_search_shape(akua_pbf* s, int32_t block, int32_t staged) {
-    if (!s || (block != 64 && block != 128 && block != 256) || (staged != 16 && staged != 32))
+    if (!s || (block != 64 && block != 128 && block != 256) ||
+        (staged != 16 && staged != 32 && staged != 48) || (staged == 48 && block == 256))
         return AKUA_ERR_INVALID_ARGUMENT;
     s->search_block = block;
     s->search_stage = staged;
@@ -1166,10 +1171,11 @@ int akua_pbf_autotune(akua_pbf* s, float dt, const float bmin[3], const float bm
     }
     // the walk's tile shape, with the pair kernels at their chosen sizes
     for (int k = 0; k < AKUA_PBF_PAIR_KERNELS; ++k) s->pair_block[k] = choice[k];
-    const int shapes[6][2] = {{128, 32}, {64, 32}, {256, 32}, {128, 16}, {64, 16}, {256, 16}};
+    const int shapes[8][2] = {{128, 32}, {64, 32}, {256, 32}, {128, 16}, {64, 16}, {256, 16},
+                              {64, 48}, {128, 48}};
     int shape_choice[2] = {s->search_block, s->search_stage};
     double shape_best = 1e30;
-    for (int c = 0; c < 6 && rc == AKUA_OK; ++c) {
+    for (int c = 0; c < 8 && rc == AKUA_OK; ++c) {
         s->search_block = shapes[c][0];
         s->search_stage = shapes[c][1];
         trial();

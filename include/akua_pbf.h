@@ -224,8 +224,8 @@ int akua_pbf_set_scene(akua_pbf* solver, int32_t scene, const akua_scene_desc* d
 int akua_pbf_set_pair_blocks(akua_pbf* solver, const int32_t blocks[AKUA_PBF_PAIR_KERNELS]);
 int akua_pbf_get_pair_blocks(akua_pbf* solver, int32_t blocks[AKUA_PBF_PAIR_KERNELS]);
 /* The neighbour walk's tile shape: its block size (64, 128 or 256 threads) and how many list
- * entries per particle it stages in shared memory before writing them out (16 or 32); lists do
- * not depend on it.  Default 128 / 32. */
+ * entries per particle it stages in shared memory before writing them out (16, 32, or 48 with 64
+ * or 128 threads); lists do not depend on it.  Default 128 / 32. */
 int akua_pbf_set_search_shape(akua_pbf* solver, int32_t block, int32_t staged);
 int akua_pbf_get_search_shape(akua_pbf* solver, int32_t* block, int32_t* staged);
 /* Autotuner: times every candidate block size of every pair kernel, then every walk tile shape,

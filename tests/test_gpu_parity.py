@@ -341,7 +341,8 @@ def test_fast_one_step_1m_full_size():
     assert_close_fast(g, o)
 
 
-@pytest.mark.parametrize("shape", [(64, 32), (256, 32), (64, 16), (128, 16), (256, 16)])
+@pytest.mark.parametrize("shape", [(64, 32), (256, 32), (64, 16), (128, 16), (256, 16), (64, 48),
+                                   (128, 48)])
 def test_walk_tile_shapes_identical(shape):
     """Every tile shape of the walk the autotuner can pick gives the default shape's records,
     lists and order bit for bit (three steps, both math modes)."""
