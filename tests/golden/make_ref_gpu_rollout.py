@@ -7,6 +7,10 @@ reference sources into cubins by oracle/ref_gpu.py, driven by oracle/ref_harness
   |x_A - x_B| and |v_A - v_B| after 1..50 steps, is the floor of the rollout tolerances.
 * tests/golden/ref_gpu_rollout_27k.npz: run A's positions and velocities after 20 and 50 steps
   of the 27k dam break, in input order (colour.r carries each particle's input index).
+* tests/golden/ref_gpu_aggregates_27k.json: whole-scene quantities of the 27k dam break every 10
+  steps over 200 steps, for two runs of the reference kernels (kinetic energy, centre of mass,
+  spread, density error): by then the flow is chaotic particle by particle, and these are what two
+  runs of the reference still agree on, and how closely.
 
 Run on a GPU machine where oracle/_ref/ holds the cubins:
 
@@ -60,6 +64,34 @@ def spread_quantiles(a, b):
             "velocity": [float(np.quantile(dv, q)) for q in QUANTILES]}
 
 
+AGG_STEPS = tuple(range(10, 201, 10))
+
+
+def aggregates(p, rho0=7600.0):
+    """Whole-scene quantities of one state (float64 sums)."""
+    x = p["position"].astype(np.float64)
+    v = p["velocity"].astype(np.float64)
+    m = p["mass"].astype(np.float64)
+    c = p["density"].astype(np.float64) / rho0 - 1.0
+    com = (m[:, None] * x).sum(0) / m.sum()
+    return {"kinetic_energy": float(0.5 * (m * (v * v).sum(1)).sum()),
+            "com_x": float(com[0]), "com_y": float(com[1]), "com_z": float(com[2]),
+            "spread_x": float(np.sqrt((m * (x[:, 0] - com[0]) ** 2).sum() / m.sum())),
+            "mean_abs_c": float(np.abs(c).mean()), "max_c": float(c.max())}
+
+
+def aggregate_runs(out_dir):
+    sc = scene.workload("dam_break_27k", seed=0)
+    cfg, corr = scene.benchmark_params()
+    runs = []
+    for _ in range(2):
+        states = run_chain(sc, cfg, corr, AGG_STEPS)
+        runs.append({str(k): aggregates(states[k], cfg.restDensity) for k in AGG_STEPS})
+    with open(os.path.join(out_dir, "ref_gpu_aggregates_27k.json"), "w") as f:
+        json.dump({"workload": "dam_break_27k", "seed": 0, "steps": list(AGG_STEPS),
+                   "runs": runs}, f, indent=1)
+
+
 def main(out_dir):
     os.makedirs(out_dir, exist_ok=True)
     spread = {"quantiles": list(QUANTILES),
@@ -82,7 +114,14 @@ def main(out_dir):
                 **{"velocity_%d" % s: run_a[s]["velocity"] for s in (20, 50)})
     with open(os.path.join(out_dir, "ref_gpu_spread.json"), "w") as f:
         json.dump(spread, f, indent=1)
+    aggregate_runs(out_dir)
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.path.join(ROOT, "tests", "golden"))
+    # python make_ref_gpu_rollout.py [out_dir [aggregates]]: with "aggregates", only that fixture
+    out = sys.argv[1] if len(sys.argv) > 1 else os.path.join(ROOT, "tests", "golden")
+    if len(sys.argv) > 2 and sys.argv[2] == "aggregates":
+        os.makedirs(out, exist_ok=True)
+        aggregate_runs(out)
+    else:
+        main(out)

@@ -17,7 +17,8 @@ Bars (every quantile 50%..100%, positions and velocities):
   * fast step vs the FP64 oracle: at most 1.5 x S_fp32 (plus the floor), i.e. the benchmarked mode
     is as accurate as the reference's own FP32 arithmetic.
 Hashes, order and lists stay bit-exact per step; exact-math mode stays bit-exact over rollouts
-(tests/test_gpu_parity.py).
+(tests/test_gpu_parity.py; 200 steps of the 27k dam break below, where the fast mode is judged on
+whole-scene quantities against two runs of the reference's kernels).
 """
 import json
 import os
@@ -108,3 +109,57 @@ def test_fast_rollout_within_reference_spread(case, snaps):
             if ref is not None and ("%s_%d" % (field, s)) in ref:
                 vs_ref = quantiles(fast[s], {field: ref["%s_%d" % (field, s)]}, field)
                 assert np.all(vs_ref <= bound), (case, s, field, "vs reference", vs_ref, bound)
+
+
+def test_200_steps_of_the_27k_dam_break(cuda_lib):
+    """The 27k dam break over 200 steps against the host oracle.  With exact math every record of
+    every one of the 200 steps equals the FP32 restatement's (checked every 10 steps).  In the
+    benchmarked fast mode the flow has long become chaotic particle by particle, so whole-scene
+    quantities are compared: kinetic energy, centre of mass, spread along x, mean and max density
+    constraint.  Correct runs scatter around each other: two runs of the reference's kernels
+    (tests/golden/ref_gpu_aggregates_27k.json) and the FP32 and FP64 restatements form the
+    ensemble; the fast step must lie within 3 x the ensemble's width plus 0.5% of its mean."""
+    import akuaengine_gb300 as ak
+    from make_ref_gpu_rollout import AGG_STEPS, aggregates
+
+    with open(os.path.join(GOLDEN, "ref_gpu_aggregates_27k.json")) as f:
+        ref = json.load(f)
+    sc = scene.workload(ref["workload"], seed=ref["seed"])
+    cfg, corr = scene.benchmark_params()
+    runs = {"refA": ref["runs"][0], "refB": ref["runs"][1]}
+    exact_mismatch = []
+    for name, flags in (("o32", oracle.FMA), ("o64", oracle.FMA | oracle.FP64)):
+        q = sc.particles.copy()
+        P = oracle.make_params(cfg, corr, sc.dt, sc.box_min, sc.box_max, n=sc.n, flags=flags)
+        g = sc.particles.copy()
+        solver = PBFSolver(sc.n, cfg, corr, options=ak.OPT_EXACT_MATH) if name == "o32" else None
+        agg = {}
+        try:
+            for k in range(1, 201):
+                oracle.step(q, P)
+                if solver is not None:
+                    solver.step_host(g, sc.dt, sc.box_min, sc.box_max)
+                if k in AGG_STEPS:
+                    agg[str(k)] = aggregates(q, cfg.restDensity)
+                    if solver is not None and g.tobytes() != q.tobytes():
+                        exact_mismatch.append(k)
+        finally:
+            if solver is not None:
+                solver.close()
+        runs[name] = agg
+    assert not exact_mismatch, "exact-math records differ from the oracle at steps %s" % exact_mismatch
+    fast, p = {}, sc.particles.copy()
+    with PBFSolver(sc.n, cfg, corr) as s:
+        for k in range(1, 201):
+            s.step_host(p, sc.dt, sc.box_min, sc.box_max)
+            if k in AGG_STEPS:
+                fast[str(k)] = aggregates(p, cfg.restDensity)
+    worst = 0.0
+    for k in map(str, AGG_STEPS):
+        for q, v in fast[k].items():
+            e = [runs[n][k][q] for n in ("refA", "refB", "o32", "o64")]
+            mid, width = sum(e) / len(e), max(e) - min(e)
+            bound = 3.0 * width + 5e-3 * abs(mid)
+            worst = max(worst, abs(v - mid) / bound)
+            assert abs(v - mid) <= bound, (k, q, v, e)
+    print("200-step aggregates: worst |fast - ensemble| / bound = %.2f" % worst)
