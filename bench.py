@@ -488,14 +488,18 @@ def run_batched(args, cfg, corr):
     prof = solver.profile_end()
     solver.close()
     kernel_sum_ms = sum(v[1] for v in prof.values()) / prof_steps
+    node_us = graph_node_us(launches)
     launch_cost = {
         "launches_per_batch_step": launches,
         "graph_step_ms": round(ms / args.steps, 4),
         "kernels_launched_one_by_one_ms": round(kernel_sum_ms, 4),
         "kernels": {k: round(1000.0 * v[1] / max(v[0], 1), 2) for k, v in prof.items()},
-        "what": "the second figure times each kernel between events with its own launch (sorts "
-                "not overlapped); a persistent kernel could save at most the graph's per-launch "
-                "gaps, launches x about a microsecond"}
+        "graph_node_us": round(node_us, 3),
+        "launch_bound_ms": round(launches * node_us / 1000.0, 4),
+        "what": "the one-by-one figure times each kernel between events with its own launch "
+                "(sorts not overlapped); graph_node_us is the replay cost per node of a CUDA graph "
+                "of as many tiny kernels, so launches x graph_node_us bounds what a persistent "
+                "kernel could save"}
     if rank == 0:
         line = {
             "metric": "batched scenes particle-steps/s", "value": round(b.n * args.steps / (ms / 1e3), 1),
@@ -520,6 +524,36 @@ def run_batched(args, cfg, corr):
             "clocks": clocks,
         }
         print(json.dumps(line), flush=True)
+
+
+def graph_node_us(nodes: int) -> float:
+    """Replay cost per node of a CUDA graph of `nodes` tiny kernels (one-element adds), launch and
+    the kernels' own run included: what each launch of a graph costs at the least."""
+    import torch
+
+    x = torch.zeros(32, device="cuda")
+    st = torch.cuda.Stream()
+    times = {}
+    for k in (1, nodes):
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(st):
+            for _ in range(k):
+                x.add_(1.0)
+            torch.cuda.synchronize()
+            with torch.cuda.graph(g, stream=st):
+                for _ in range(k):
+                    x.add_(1.0)
+        torch.cuda.synchronize()
+        for _ in range(20):
+            g.replay()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(200):
+            g.replay()
+        e1.record()
+        torch.cuda.synchronize()
+        times[k] = e0.elapsed_time(e1) / 200 * 1000.0
+    return (times[nodes] - times[1]) / max(nodes - 1, 1)
 
 
 def replicas_seed(rank):
